@@ -1,0 +1,127 @@
+"""ctypes bindings of libedgeloops.so (the C ABI in include/edge_loops.h).
+
+The library is loaded from this package's folder.  There is no fallback: if
+the shared object is missing, loading raises, so nothing can silently run
+another implementation.
+"""
+import ctypes as C
+import os
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libedgeloops.so")
+
+# ---- enums / flags (mirror include/edge_loops.h) ---------------------------
+EL_OK = 0
+EL_ERR_INVALID_ARGUMENT = 1
+EL_ERR_NULL_POINTER = 2
+EL_ERR_OVERFLOW = 3
+EL_ERR_UNSUPPORTED = 4
+EL_ERR_MALFORMED_CSR = 5
+EL_ERR_CUDA = 6
+EL_ERR_OUT_OF_MEMORY = 7
+EL_ERR_DEVICE = 8
+
+EL_F32, EL_BF16, EL_F16 = 0, 1, 2
+
+EL_SCHED_MERGE_PATH_FLAT = 0
+EL_SCHED_WORK_ORIENTED = 1
+EL_SCHED_THREAD_MAPPED = 2
+EL_SCHED_GROUP_MAPPED = 3
+EL_SCHED_BUCKETING = 4
+EL_SCHED_AUTO = 5
+
+EL_FLAG_INDEX_RANGE = 0x1
+EL_FLAG_OFFSETS = 0x2
+EL_FLAG_NNZ_MISMATCH = 0x4
+EL_FLAG_TIMEOUT = 0x8
+
+
+class ElCsr(C.Structure):
+    _fields_ = [
+        ("rows", C.c_int64),
+        ("cols", C.c_int64),
+        ("nnz", C.c_int64),
+        ("offsets", C.c_void_p),
+        ("indices", C.c_void_p),
+        ("values", C.c_void_p),
+        ("value_dtype", C.c_int32),
+        ("reserved0", C.c_int32),
+        ("row_scale", C.c_void_p),
+    ]
+
+
+class ElSpmvOpts(C.Structure):
+    _fields_ = [
+        ("threads_per_block", C.c_int32),
+        ("items_per_thread", C.c_int32),
+        ("threads_per_row", C.c_int32),
+        ("group_rows", C.c_int32),
+        ("num_threads", C.c_int64),
+        ("compensated", C.c_int32),
+        ("max_ctas", C.c_int32),
+        ("wait_limit_us", C.c_int32),
+        ("test_hooks", C.c_int32),
+        ("reserved", C.c_int32 * 6),
+    ]
+
+
+# name -> (restype, argtypes); every symbol include/edge_loops.h declares
+SIGNATURES = {
+    "el_version": (C.c_int, []),
+    "el_status_string": (C.c_char_p, [C.c_int]),
+    "el_last_error_string": (C.c_char_p, []),
+    "el_spmv_opts_default": (None, [C.POINTER(ElSpmvOpts)]),
+    "el_workspace_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    "el_workspace_destroy": (C.c_int, [C.c_void_p]),
+    "el_workspace_errors": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint32), C.c_int]),
+    "el_spmv": (C.c_int, [C.c_void_p, C.POINTER(ElCsr), C.c_int32, C.POINTER(ElSpmvOpts),
+                          C.c_void_p, C.c_void_p, C.c_void_p]),
+    "el_spmm": (C.c_int, [C.c_void_p, C.POINTER(ElCsr), C.c_int32, C.POINTER(ElSpmvOpts),
+                          C.c_void_p, C.c_int32, C.c_int64, C.c_int64, C.c_void_p, C.c_int64,
+                          C.c_void_p]),
+    "el_csr_validate": (C.c_int, [C.POINTER(ElCsr), C.c_void_p, C.POINTER(C.c_uint32)]),
+    "el_merge_path_num_tiles": (C.c_int64, [C.c_int64, C.c_int64, C.c_int32, C.c_int32]),
+    "el_merge_path_partition": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int32,
+                                          C.c_int32, C.c_void_p, C.c_void_p]),
+    "el_merge_path_thread_coords": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int32,
+                                              C.c_int32, C.c_void_p, C.c_void_p]),
+    "el_work_oriented_partition": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_int64,
+                                             C.c_void_p, C.c_void_p]),
+    "el_quantize_values": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_int32,
+                                     C.c_void_p, C.c_void_p, C.c_void_p]),
+}
+
+_lib = None
+
+
+def lib():
+    """Loads libedgeloops.so once (raises OSError if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError(
+                "libedgeloops.so is not built (run `python -m edge_loops_gb300.build`); "
+                "there is no fallback implementation")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+class ElError(RuntimeError):
+    """A non-EL_OK status from the C ABI."""
+
+    def __init__(self, status, where):
+        L = lib()
+        self.status = status
+        name = L.el_status_string(status).decode()
+        msg = L.el_last_error_string().decode()
+        super().__init__(f"{where}: {name}: {msg}")
+
+
+def check(status, where):
+    if status != EL_OK:
+        raise ElError(status, where)

@@ -1,0 +1,233 @@
+"""Python face of the C ABI: CSR matrices held in torch device tensors, and
+the reference's entry points (spmv / spmm per schedule) as functions.
+
+Everything computed here runs in libedgeloops.so; torch only provides device
+memory and the current CUDA stream.  The schedule names are the reference's
+(loops::schedule::algorithms_t, include/loops/schedule.hxx:23-29, and the
+entry points of include/loops/algorithms/spmv/*.cuh): "merge_path_flat"
+(alias "merge_path"), "work_oriented", "thread_mapped" (alias "original"),
+"group_mapped", plus "auto".
+"""
+import ctypes as C
+
+import torch
+
+from . import _lib as L
+
+SCHEDULES = {
+    "merge_path_flat": L.EL_SCHED_MERGE_PATH_FLAT,
+    "merge_path": L.EL_SCHED_MERGE_PATH_FLAT,
+    "work_oriented": L.EL_SCHED_WORK_ORIENTED,
+    "thread_mapped": L.EL_SCHED_THREAD_MAPPED,
+    "original": L.EL_SCHED_THREAD_MAPPED,
+    "group_mapped": L.EL_SCHED_GROUP_MAPPED,
+    "bucketing": L.EL_SCHED_BUCKETING,
+    "auto": L.EL_SCHED_AUTO,
+}
+
+_DT = {torch.float32: L.EL_F32, torch.bfloat16: L.EL_BF16, torch.float16: L.EL_F16}
+_DT_BY_CODE = {v: k for k, v in _DT.items()}
+
+
+def _ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _stream(stream):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _sched(schedule):
+    if isinstance(schedule, int):
+        return schedule
+    try:
+        return SCHEDULES[schedule]
+    except KeyError:
+        raise ValueError(f"unknown schedule {schedule!r}; one of {sorted(SCHEDULES)}")
+
+
+class CSR:
+    """A CSR matrix in device memory (the reference's csr_t,
+    include/loops/container/csr.hxx:32-95): int32 offsets (rows+1), int32
+    column indices and values (float32, bfloat16 or float16), with an
+    optional float32 per-row scale (A[i, j] = row_scale[i] * values[ij])."""
+
+    def __init__(self, offsets, indices, values, rows, cols, row_scale=None):
+        self.offsets = offsets
+        self.indices = indices
+        self.values = values
+        self.rows = int(rows)
+        self.cols = int(cols)
+        self.row_scale = row_scale
+        if values.dtype not in _DT:
+            raise TypeError(f"values dtype {values.dtype} not supported")
+
+    @property
+    def nnz(self):
+        return int(self.indices.numel())
+
+    @property
+    def nnzs(self):  # the reference's field name
+        return self.nnz
+
+    @property
+    def device(self):
+        return self.offsets.device
+
+    def el(self):
+        s = L.ElCsr()
+        s.rows, s.cols, s.nnz = self.rows, self.cols, self.nnz
+        s.offsets = self.offsets.data_ptr()
+        s.indices = self.indices.data_ptr() if self.nnz else None
+        s.values = self.values.data_ptr() if self.nnz else None
+        s.value_dtype = _DT[self.values.dtype]
+        s.row_scale = self.row_scale.data_ptr() if self.row_scale is not None else None
+        return s
+
+    @classmethod
+    def from_arrays(cls, offsets, indices, values, cols, device="cuda", rows=None):
+        """From numpy/torch host arrays (copied to `device`)."""
+        off = torch.as_tensor(offsets, dtype=torch.int32).to(device)
+        idx = torch.as_tensor(indices, dtype=torch.int32).to(device)
+        val = torch.as_tensor(values).to(device)
+        r = int(off.numel() - 1) if rows is None else int(rows)
+        return cls(off, idx, val, r, cols)
+
+    def quantized(self, dtype, per_row_scale=True, stream=None):
+        """BF16/FP16 copy of an FP32 matrix (el_quantize_values); with
+        per_row_scale each row is scaled by a power of two into [1, 2)."""
+        if self.values.dtype != torch.float32:
+            raise TypeError("quantize an FP32 matrix")
+        out = torch.empty(self.nnz, dtype=dtype, device=self.device)
+        scale = torch.empty(self.rows, dtype=torch.float32, device=self.device) \
+            if per_row_scale else None
+        L.check(L.lib().el_quantize_values(
+            _ptr(self.offsets), self.rows, self.nnz, _ptr(self.values), _DT[dtype],
+            _ptr(out), _ptr(scale), _stream(stream)), "el_quantize_values")
+        return CSR(self.offsets, self.indices, out, self.rows, self.cols, row_scale=scale)
+
+
+class Workspace:
+    """An el_workspace (device state of the persistent schedules)."""
+
+    def __init__(self, device=None):
+        dev = torch.cuda.current_device() if device is None else int(device)
+        h = C.c_void_p()
+        L.check(L.lib().el_workspace_create(dev, C.byref(h)), "el_workspace_create")
+        self.handle = h
+
+    def errors(self, clear=True, stream=None):
+        return workspace_errors(self, clear=clear, stream=stream)
+
+    def close(self):
+        if self.handle:
+            L.lib().el_workspace_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _ws(ws):
+    return None if ws is None else ws.handle
+
+
+def workspace_errors(ws=None, clear=True, stream=None):
+    """Device error flags (EL_FLAG_*) of a workspace, or of the library's
+    workspace for the current device and stream when ws is None."""
+    f = C.c_uint32(0)
+    L.check(L.lib().el_workspace_errors(_ws(ws), _stream(stream), C.byref(f), int(clear)),
+            "el_workspace_errors")
+    return int(f.value)
+
+
+def make_opts(threads_per_block=0, items_per_thread=0, threads_per_row=0, group_rows=0,
+              num_threads=0, compensated=False, max_ctas=0, wait_limit_us=0):
+    o = L.ElSpmvOpts()
+    L.lib().el_spmv_opts_default(C.byref(o))
+    o.threads_per_block = threads_per_block
+    o.items_per_thread = items_per_thread
+    o.threads_per_row = threads_per_row
+    o.group_rows = group_rows
+    o.num_threads = num_threads
+    o.compensated = int(bool(compensated))
+    o.max_ctas = max_ctas
+    o.wait_limit_us = wait_limit_us
+    return o
+
+
+def spmv(A, x, y=None, schedule="merge_path_flat", stream=None, workspace=None, **opts):
+    """y = A x (y overwritten), the reference's
+    loops::algorithms::spmv::<schedule>(csr, x, y, stream)."""
+    if y is None:
+        y = torch.empty(A.rows, dtype=torch.float32, device=A.device)
+    if x.dtype != torch.float32 or y.dtype != torch.float32:
+        raise TypeError("x and y are float32")
+    if x.numel() < A.cols or y.numel() < A.rows:
+        raise ValueError("x or y too short")
+    a = A.el()
+    o = make_opts(**opts)
+    L.check(L.lib().el_spmv(_ws(workspace), C.byref(a), _sched(schedule), C.byref(o),
+                            _ptr(x), _ptr(y), _stream(stream)), "el_spmv")
+    return y
+
+
+def spmm(A, B, Cm=None, schedule="merge_path_flat", stream=None, workspace=None, **opts):
+    """C = A B with B row-major (cols x n) float32/bfloat16/float16 and C
+    float32 (rows x n), the reference's loops::algorithms::spmm."""
+    if B.dim() != 2 or B.shape[0] != A.cols or B.stride(1) != 1:
+        raise ValueError("B must be a row-major (cols x n) matrix")
+    n = B.shape[1]
+    if Cm is None:
+        Cm = torch.empty(A.rows, n, dtype=torch.float32, device=A.device)
+    if Cm.dtype != torch.float32 or Cm.stride(1) != 1 or Cm.shape != (A.rows, n):
+        raise ValueError("C must be float32 row-major (rows x n)")
+    a = A.el()
+    o = make_opts(**opts)
+    L.check(L.lib().el_spmm(_ws(workspace), C.byref(a), _sched(schedule), C.byref(o),
+                            _ptr(B), _DT[B.dtype], n, B.stride(0), _ptr(Cm), Cm.stride(0),
+                            _stream(stream)), "el_spmm")
+    return Cm
+
+
+def validate(A, stream=None):
+    """Returns the EL_FLAG_* defects of A (0 for a well-formed CSR)."""
+    a = A.el()
+    f = C.c_uint32(0)
+    st = L.lib().el_csr_validate(C.byref(a), _stream(stream), C.byref(f))
+    if st not in (L.EL_OK, L.EL_ERR_MALFORMED_CSR):
+        L.check(st, "el_csr_validate")
+    return int(f.value)
+
+
+def merge_path_partition(offsets, rows, nnz, tpb=128, ipt=5, stream=None):
+    """Tile start coordinates (row, nonzero) at diagonals k*tpb*ipt plus the
+    end of the last tile: uint32 tensor of shape (tiles+1, 2)."""
+    tiles = int(L.lib().el_merge_path_num_tiles(rows, nnz, tpb, ipt))
+    out = torch.empty((tiles + 1) * 2, dtype=torch.int32, device=offsets.device)
+    L.check(L.lib().el_merge_path_partition(_ptr(offsets), rows, nnz, tpb, ipt, _ptr(out),
+                                            _stream(stream)), "el_merge_path_partition")
+    return out.view(tiles + 1, 2)
+
+
+def merge_path_thread_coords(offsets, rows, nnz, tpb=128, ipt=5, stream=None):
+    """Per (tile, thread) local start coordinate: shape (tiles, tpb, 2)."""
+    tiles = int(L.lib().el_merge_path_num_tiles(rows, nnz, tpb, ipt))
+    out = torch.empty(max(tiles, 1) * tpb * 2, dtype=torch.int32, device=offsets.device)
+    L.check(L.lib().el_merge_path_thread_coords(_ptr(offsets), rows, nnz, tpb, ipt,
+                                                _ptr(out), _stream(stream)),
+            "el_merge_path_thread_coords")
+    return out[: tiles * tpb * 2].view(tiles, tpb, 2)
+
+
+def work_oriented_partition(offsets, rows, nnz, num_threads, stream=None):
+    """Per thread (start row, start nz, end row, end nz): shape (num_threads, 4)."""
+    out = torch.empty(num_threads * 4, dtype=torch.int64, device=offsets.device)
+    L.check(L.lib().el_work_oriented_partition(_ptr(offsets), rows, nnz, num_threads,
+                                               _ptr(out), _stream(stream)),
+            "el_work_oriented_partition")
+    return out.view(num_threads, 4)

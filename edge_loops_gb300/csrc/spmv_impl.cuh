@@ -1,0 +1,156 @@
+// spmv_impl.cuh -- per-value-type launchers of the four SpMV schedules.
+// Included once per value type (spmv_f32.cu, spmv_bf16.cu, spmv_f16.cu) so
+// the heavy template instantiations compile in parallel.
+#pragma once
+
+#include "spmv_merge_path.cuh"
+#include "spmv_schedules.cuh"
+
+namespace el {
+
+template <typename VT>
+struct SpmvImpl {
+  static el_status merge_path(const SpmvCall& c) {
+    const int ipt = c.o.items_per_thread;
+    const bool comp = c.o.compensated != 0;
+    if (ipt > 0 && ipt <= 4)
+      return comp ? mp::launch<VT, 4, true>(c) : mp::launch<VT, 4, false>(c);
+    return comp ? mp::launch<VT, 8, true>(c) : mp::launch<VT, 8, false>(c);
+  }
+  static long long merge_path_slots(const SpmvCall& c) {
+    const int ipt = c.o.items_per_thread;
+    const bool comp = c.o.compensated != 0;
+    if (ipt > 0 && ipt <= 4)
+      return comp ? mp::slots_needed<VT, 4, true>(c) : mp::slots_needed<VT, 4, false>(c);
+    return comp ? mp::slots_needed<VT, 8, true>(c) : mp::slots_needed<VT, 8, false>(c);
+  }
+
+  static BasicArgs basic(const SpmvCall& c) {
+    BasicArgs a;
+    a.rows = c.A.rows;
+    a.cols = c.A.cols;
+    a.nnz = c.A.nnz;
+    a.offsets = c.A.offsets;
+    a.indices = c.A.indices;
+    a.values = c.A.values;
+    a.row_scale = c.A.row_scale;
+    a.x = c.x;
+    a.y = c.y;
+    a.hdr = c.ws.hdr;
+    return a;
+  }
+
+  template <int TPR, bool COMP>
+  static el_status tm(const SpmvCall& c) {
+    const int tpb = 256;
+    long long grid = (c.A.rows * TPR + tpb - 1) / tpb;
+    const long long cap = (long long)device_info(c.device).sm_count * 32;
+    if (grid > cap) grid = cap;
+    if (grid < 1) grid = 1;
+    thread_mapped_spmv_kernel<VT, TPR, COMP><<<(unsigned)grid, tpb, 0, c.stream>>>(basic(c));
+    return cuda_status(cudaGetLastError(), "thread_mapped launch");
+  }
+  template <bool COMP>
+  static el_status tm_tpr(const SpmvCall& c) {
+    switch (c.o.threads_per_row) {
+      case 0:
+      case 1: return tm<1, COMP>(c);
+      case 2: return tm<2, COMP>(c);
+      case 4: return tm<4, COMP>(c);
+      case 8: return tm<8, COMP>(c);
+      case 16: return tm<16, COMP>(c);
+      case 32: return tm<32, COMP>(c);
+    }
+    return fail(EL_ERR_INVALID_ARGUMENT, "threads_per_row must be 1,2,4,8,16 or 32");
+  }
+  static el_status thread_mapped(const SpmvCall& c) {
+    return c.o.compensated ? tm_tpr<true>(c) : tm_tpr<false>(c);
+  }
+
+  template <int GT, int TPB, bool COMP>
+  static el_status gm(const SpmvCall& c) {
+    constexpr int NG = TPB / GT;
+    const long long groups = (c.A.rows + GT - 1) / GT;
+    long long grid = (groups + NG - 1) / NG;
+    const long long cap = (long long)device_info(c.device).sm_count * 32;
+    if (grid > cap) grid = cap;
+    if (grid < 1) grid = 1;
+    group_mapped_spmv_kernel<VT, GT, TPB, COMP><<<(unsigned)grid, TPB, 0, c.stream>>>(basic(c));
+    return cuda_status(cudaGetLastError(), "group_mapped launch");
+  }
+  template <bool COMP>
+  static el_status gm_cfg(const SpmvCall& c) {
+    const int tpb = c.o.threads_per_block > 0 ? c.o.threads_per_block : 128;
+    const int rows = c.o.group_rows > 0 ? c.o.group_rows : tpb;
+    if (rows == 32) return gm<32, 256, COMP>(c);
+    if (rows == 128 && tpb == 128) return gm<128, 128, COMP>(c);
+    if (rows == 256 && tpb == 256) return gm<256, 256, COMP>(c);
+    return fail(EL_ERR_INVALID_ARGUMENT,
+                "group_mapped: group_rows 32 (warp groups) or == threads_per_block "
+                "in {128, 256}");
+  }
+  static el_status group_mapped(const SpmvCall& c) {
+    return c.o.compensated ? gm_cfg<true>(c) : gm_cfg<false>(c);
+  }
+
+  static constexpr int kWoTpb = 128;
+  static long long wo_num_threads(const SpmvCall& c) {
+    if (c.o.num_threads > 0) return c.o.num_threads;
+    // the reference launches 2 x SM count blocks of 128
+    return 2LL * device_info(c.device).sm_count * kWoTpb;
+  }
+  static long long work_oriented_slots(const SpmvCall& c) {
+    return (wo_num_threads(c) + kWoTpb - 1) / kWoTpb;
+  }
+  template <bool COMP>
+  static el_status wo(const SpmvCall& c) {
+    const long long nt = wo_num_threads(c);
+    if (nt % kWoTpb != 0)
+      return fail(EL_ERR_INVALID_ARGUMENT, "work_oriented: num_threads must be a multiple of %d",
+                  kWoTpb);
+    WoArgs w;
+    w.b = basic(c);
+    const long long total = c.A.rows + c.A.nnz;
+    w.wpt = (total + nt - 1) / nt;
+    if (w.wpt < 1) w.wpt = 1;
+    w.num_blocks = (int)(nt / kWoTpb);
+    w.wait_ns = c.wait_ns;
+    w.ws = c.ws;
+    if (w.num_blocks > c.ws.nslots)
+      return fail(EL_ERR_INVALID_ARGUMENT, "work_oriented: workspace too small");
+    work_oriented_spmv_kernel<VT, kWoTpb, COMP><<<w.num_blocks, kWoTpb, 0, c.stream>>>(w);
+    return cuda_status(cudaGetLastError(), "work_oriented launch");
+  }
+  static el_status work_oriented(const SpmvCall& c) {
+    return c.o.compensated ? wo<true>(c) : wo<false>(c);
+  }
+};
+
+template <typename VT> el_status spmv_merge_path(const SpmvCall& c) {
+  return SpmvImpl<VT>::merge_path(c);
+}
+template <typename VT> long long spmv_merge_path_slots(const SpmvCall& c) {
+  return SpmvImpl<VT>::merge_path_slots(c);
+}
+template <typename VT> el_status spmv_thread_mapped(const SpmvCall& c) {
+  return SpmvImpl<VT>::thread_mapped(c);
+}
+template <typename VT> el_status spmv_group_mapped(const SpmvCall& c) {
+  return SpmvImpl<VT>::group_mapped(c);
+}
+template <typename VT> el_status spmv_work_oriented(const SpmvCall& c) {
+  return SpmvImpl<VT>::work_oriented(c);
+}
+template <typename VT> long long spmv_work_oriented_slots(const SpmvCall& c) {
+  return SpmvImpl<VT>::work_oriented_slots(c);
+}
+
+#define EL_INSTANTIATE_SPMV(VT)                                          \
+  template el_status spmv_merge_path<VT>(const SpmvCall&);               \
+  template long long spmv_merge_path_slots<VT>(const SpmvCall&);         \
+  template el_status spmv_thread_mapped<VT>(const SpmvCall&);            \
+  template el_status spmv_group_mapped<VT>(const SpmvCall&);             \
+  template el_status spmv_work_oriented<VT>(const SpmvCall&);            \
+  template long long spmv_work_oriented_slots<VT>(const SpmvCall&);
+
+}  // namespace el

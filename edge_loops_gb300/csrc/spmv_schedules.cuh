@@ -1,0 +1,353 @@
+// spmv_schedules.cuh -- the thread_mapped, group_mapped and work_oriented
+// SpMV schedules for sm_103a.  All three overwrite y and are deterministic.
+#pragma once
+
+#include "el_internal.h"
+
+namespace el {
+
+struct BasicArgs {
+  long long rows, cols, nnz;
+  const int* offsets;
+  const int* indices;
+  const void* values;
+  const float* row_scale;
+  const float* x;
+  float* y;
+  WsHeader* hdr;
+};
+
+__device__ __forceinline__ void row_bounds(const BasicArgs& a, long long row,
+                                           long long* b, long long* e) {
+  long long lo = __ldg(a.offsets + row), hi = __ldg(a.offsets + row + 1);
+  if (lo < 0 || hi > a.nnz || hi < lo) {
+    raise_flag(a.hdr, EL_FLAG_OFFSETS, (unsigned)row);
+    lo = lo < 0 ? 0 : (lo > a.nnz ? a.nnz : lo);
+    hi = hi < lo ? lo : (hi > a.nnz ? a.nnz : hi);
+  }
+  *b = lo;
+  *e = hi;
+}
+
+template <typename VT>
+__device__ __forceinline__ float product(const BasicArgs& a, long long nz) {
+  const int col = __ldg(a.indices + nz);
+  if ((unsigned)col >= (unsigned long long)a.cols) {
+    raise_flag(a.hdr, EL_FLAG_INDEX_RANGE, (unsigned)nz);
+    return 0.f;
+  }
+  return __fmul_rn(to_f32(reinterpret_cast<const VT*>(a.values)[nz]),
+                   __ldg(a.x + col));
+}
+
+__device__ __forceinline__ float scaled(const BasicArgs& a, long long row,
+                                        float v) {
+  return a.row_scale ? v * __ldg(a.row_scale + row) : v;
+}
+
+// ------------------------------------------------------------ thread_mapped
+// The reference's thread_mapped / original schedule
+// [include/loops/schedule/thread_mapped.hxx:147-160,
+//  include/loops/algorithms/spmv/thread_mapped.cuh:26-55]: rows in a grid-
+// stride loop, each summed in nonzero order.  TPR > 1 generalises it to
+// TPR lanes per row (lane k takes nonzeros k, k+TPR, ...; lanes combine in
+// a fixed xor tree).  With TPR == 1 every row is the reference CPU loop's
+// exact sequence of FP32 roundings (no fused multiply-add).
+template <typename VT, int TPR, bool COMP>
+__global__ void __launch_bounds__(256)
+    thread_mapped_spmv_kernel(const BasicArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int sub = lane % TPR;
+  constexpr int RPW = 32 / TPR;  // rows per warp per step
+  const long long warp_id = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long base = warp_id * RPW; base < a.rows; base += nwarps * RPW) {
+    const long long row = base + lane / TPR;
+    Acc<COMP> acc;
+    if (row < a.rows) {
+      long long b, e;
+      row_bounds(a, row, &b, &e);
+      for (long long nz = b + sub; nz < e; nz += TPR) acc.add(product<VT>(a, nz));
+    }
+#pragma unroll
+    for (int d = TPR / 2; d > 0; d >>= 1) {
+      Acc<COMP> o;
+      o.set(__shfl_xor_sync(kFullMask, acc.s, d),
+            __shfl_xor_sync(kFullMask, acc.comp(), d));
+      if ((sub & d) == 0) {
+        acc.add(o);
+      } else {
+        o.add(acc);
+        acc = o;
+      }
+    }
+    if (sub == 0 && row < a.rows) a.y[row] = scaled(a, row, acc.value());
+  }
+}
+
+// ------------------------------------------------------------- group_mapped
+// The reference's group_mapped schedule [include/loops/schedule/
+// group_mapped.hxx:146-235, include/loops/algorithms/spmv/group_mapped.cuh:
+// 26-60]: a group of GT threads owns GT consecutive rows (GT = 32 is the
+// reference's warp_mapped, GT = block size its block_mapped); the group scans
+// its rows' lengths and its threads stride over the group's nonzeros, each
+// mapping its nonzero to a row by an upper bound in that scan.  Instead of
+// one atomicAdd per nonzero, every chunk of GT nonzeros is reduced by a
+// segmented scan and each row's chunk total is added once, in chunk order,
+// to a shared-memory row accumulator.
+template <typename VT, int GT, int TPB, bool COMP>
+__global__ void __launch_bounds__(TPB)
+    group_mapped_spmv_kernel(const BasicArgs a) {
+  static_assert(GT == 32 || GT == TPB, "warp groups or one block group");
+  constexpr int NG = TPB / GT;
+  __shared__ int s_off[NG][GT + 1];
+  __shared__ float s_acc[NG][GT];
+  __shared__ float s_accc[NG][COMP ? GT : 1];
+  __shared__ SegScratch<GT / 32> s_scan;
+  const int grp = threadIdx.x / GT;
+  const int t = threadIdx.x % GT;
+  auto gsync = [&]() {
+    if (GT == 32) __syncwarp(); else __syncthreads();
+  };
+  const long long ngroups = (a.rows + GT - 1) / GT;
+  // block-uniform loop over groups
+  for (long long g0 = (long long)blockIdx.x * NG; g0 < ngroups;
+       g0 += (long long)gridDim.x * NG) {
+    const long long g = g0 + grp;
+    const long long r0 = g * GT;
+    const int glen = g < ngroups ? (int)((a.rows - r0 < GT) ? a.rows - r0 : GT) : 0;
+    for (int k = t; k <= glen; k += GT) {
+      long long v = __ldg(a.offsets + r0 + k);
+      if (v < 0 || v > a.nnz) {
+        raise_flag(a.hdr, EL_FLAG_OFFSETS, (unsigned)(r0 + k));
+        v = v < 0 ? 0 : a.nnz;
+      }
+      s_off[grp][k] = (int)v;
+    }
+    s_acc[grp][t] = 0.f;
+    if (COMP) s_accc[grp][t] = 0.f;
+    gsync();
+    const long long abeg = glen > 0 ? s_off[grp][0] : 0;
+    long long aend = glen > 0 ? s_off[grp][glen] : 0;
+    if (aend < abeg) aend = abeg;
+    // group-uniform loop over chunks of GT nonzeros
+    for (long long base = abeg; base < aend; base += GT) {
+      const long long nz = base + t;
+      SegVal<COMP> mine;
+      int key = GT;  // sentinel for threads past the group's nonzeros
+      mine.f = 1;
+      bool tail = false;
+      if (nz < aend) {
+        int lo = 0, hi = glen + 1;  // upper_bound over s_off[0..glen]
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (nz < s_off[grp][mid]) hi = mid; else lo = mid + 1;
+        }
+        key = lo - 1;
+        if (key < 0) key = 0;
+        if (key > glen - 1) key = glen - 1;
+        mine.f = (t == 0) || (nz == s_off[grp][key]);
+        mine.v.add(product<VT>(a, nz));
+        tail = (t == GT - 1) || (nz + 1 == aend) || (nz + 1 >= s_off[grp][key + 1]);
+      }
+      SegVal<COMP> inc;
+      if (GT == 32) {
+        inc = warp_seg_scan<COMP>(mine);
+      } else {
+        SegVal<COMP> zero, tot;
+        zero.f = 0;
+        const SegVal<COMP> ex =
+            block_seg_scan_excl<GT / 32, COMP>(mine, zero, &s_scan, 1, &tot);
+        inc = seg_combine(ex, mine);
+      }
+      if (tail) {  // one tail per row per chunk: no two threads collide
+        Acc<COMP> acc;
+        acc.set(s_acc[grp][key], COMP ? s_accc[grp][key] : 0.f);
+        acc.add(inc.v);
+        s_acc[grp][key] = acc.s;
+        if (COMP) s_accc[grp][key] = acc.comp();
+      }
+      gsync();
+    }
+    gsync();
+    if (t < glen) {
+      Acc<COMP> acc;
+      acc.set(s_acc[grp][t], COMP ? s_accc[grp][t] : 0.f);
+      a.y[r0 + t] = scaled(a, r0 + t, acc.value());
+    }
+    gsync();
+  }
+}
+
+// ------------------------------------------------------------ work_oriented
+// The reference's work_oriented schedule [include/loops/schedule/
+// work_oriented.hxx:141-195, include/loops/algorithms/spmv/work_oriented.cuh:
+// 34-78]: num_threads threads each take an even share
+// ceil((rows+nnz)/num_threads) of the merge path, found by two searches on
+// the global row offsets, and walk it straight from global memory, complete
+// rows first, then the partial last row.  The reference stores complete rows
+// and atomically adds the partial one, which races with another block's store
+// of the same row; here partial rows are stitched by a block-wide segmented
+// scan and, across blocks, by the carry look-back of the merge-path kernel.
+struct WoArgs {
+  BasicArgs b;
+  long long wpt;  // merge items per thread
+  int num_blocks;
+  unsigned long long wait_ns;
+  WsView ws;
+};
+
+template <int NW>
+struct WoCtl {
+  int blk;
+  int pend;
+  float pend_s, pend_c;
+  SegScratch<NW> scan;
+};
+
+template <typename VT, int TPB, bool COMP>
+__global__ void __launch_bounds__(TPB)
+    work_oriented_spmv_kernel(const WoArgs w) {
+  const BasicArgs& a = w.b;
+  __shared__ WoCtl<TPB / 32> ctl;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    ctl.blk = (int)atomicAdd(&w.ws.hdr->ticket, 1u);
+    ctl.pend = 0;
+  }
+  __syncthreads();
+  const int blk = ctl.blk;
+  const bool active = blk < w.num_blocks;
+  const long long total = a.rows + a.nnz;
+  const long long tid = (long long)blk * TPB + threadIdx.x;
+  long long upper = active ? w.wpt * tid : total;
+  if (upper > total) upper = total;
+  long long lower = upper + w.wpt;
+  if (lower > total) lower = total;
+  auto row_end = [&](long long k) { return __ldg(a.offsets + 1 + k); };
+  long long sx = seq_merge_search(row_end, a.rows, 0, a.nnz, upper);
+  long long sy = upper - sx;
+  if (sx > a.rows) sx = a.rows;
+  long long ex = seq_merge_search(row_end, a.rows, 0, a.nnz, lower);
+  long long ey = lower - ex;
+  if (ex > a.rows) ex = a.rows;
+
+  Acc<COMP> run, first_v;
+  long long first_row = -1;
+  long long nz = sy;
+  for (long long row = sx; row < ex; ++row) {
+    long long e = __ldg(a.offsets + row + 1);
+    if (e > ey || e < nz) {
+      raise_flag(a.hdr, EL_FLAG_OFFSETS, (unsigned)row);
+      e = e > ey ? ey : nz;
+    }
+    for (; nz < e; ++nz) run.add(product<VT>(a, nz));
+    if (first_row < 0) {
+      first_row = row;
+      first_v = run;
+    } else {
+      a.y[row] = scaled(a, row, run.value());
+    }
+    run = Acc<COMP>();
+  }
+  for (; nz < ey; ++nz) run.add(product<VT>(a, nz));
+
+  SegVal<COMP> mine, zero, tot;
+  mine.f = first_row >= 0;
+  mine.v = run;
+  zero.f = 0;
+  const SegVal<COMP> exs =
+      block_seg_scan_excl<TPB / 32, COMP>(mine, zero, &ctl.scan, 1, &tot);
+  // block range start = thread 0's start; does it begin inside a row?
+  __shared__ long long s_bs[2];
+  if (threadIdx.x == 0) {
+    s_bs[0] = sx;
+    s_bs[1] = sy;
+  }
+  __syncthreads();
+  const long long rs = s_bs[0], ns = s_bs[1];
+  const int off_rs = rs < a.rows ? __ldg(a.offsets + rs) : (int)a.nnz;
+  const bool need_lb = active && ns > off_rs;
+  if (first_row >= 0) {
+    Acc<COMP> v = exs.v;
+    v.add(first_v);
+    if (need_lb && !exs.f && first_row == rs) {
+      ctl.pend = 1;
+      ctl.pend_s = v.s;
+      ctl.pend_c = v.comp();
+    } else {
+      a.y[first_row] = scaled(a, first_row, v.value());
+    }
+  }
+  // the block's last thread publishes the partial of its open row
+  if (active && threadIdx.x == TPB - 1) {
+    const long long re = ex, ne = ey;
+    if (re < a.rows) {
+      const long long off_re = __ldg(a.offsets + re);
+      const long long lo = off_re > ns ? off_re : ns;
+      if (ne > lo && blk < w.ws.nslots) {
+        CarrySlot* sl = w.ws.slots + blk;
+        sl->sum = tot.v.s;
+        sl->comp = tot.v.comp();
+        st_release_u32(&sl->flag, 1u);
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 32 && ctl.pend) {
+    const long long range_items = w.wpt * TPB;
+    const long long gfirst = (rs + off_rs) / range_items;
+    Acc<COMP> acc;
+    bool ok = true;
+    for (long long k = gfirst + lane; k < blk && k < w.ws.nslots; k += 32) {
+      CarrySlot* sl = w.ws.slots + k;
+      if (ld_acquire_u32(&sl->flag) == 0u) {
+        const uint64_t t0 = global_timer_ns();
+        while (ld_acquire_u32(&sl->flag) == 0u) {
+          if (global_timer_ns() - t0 > w.wait_ns) {
+            ok = false;
+            break;
+          }
+          __nanosleep(100);
+        }
+      }
+      if (!ok) break;
+      Acc<COMP> v;
+      v.set(__ldcg(&sl->sum), __ldcg(&sl->comp));
+      acc.add(v);
+      sl->flag = 0u;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      Acc<COMP> o;
+      o.set(__shfl_xor_sync(kFullMask, acc.s, d),
+            __shfl_xor_sync(kFullMask, acc.comp(), d));
+      if ((lane & d) == 0) {
+        acc.add(o);
+      } else {
+        o.add(acc);
+        acc = o;
+      }
+    }
+    ok = __all_sync(kFullMask, ok);
+    if (lane == 0) {
+      if (!ok) raise_flag(a.hdr, EL_FLAG_TIMEOUT, 5);
+      Acc<COMP> p;
+      p.set(ctl.pend_s, ctl.pend_c);
+      acc.add(p);
+      a.y[rs] = scaled(a, rs, acc.value());
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(&w.ws.hdr->done, 1u);
+    if (prev == gridDim.x - 1) {
+      atomicExch(&w.ws.hdr->ticket, 0u);
+      atomicExch(&w.ws.hdr->done, 0u);
+      __threadfence();
+    }
+  }
+}
+
+}  // namespace el

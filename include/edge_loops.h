@@ -1,0 +1,216 @@
+/*
+ * edge_loops.h -- C ABI of the GB300-native load-balanced CSR SpMV/SpMM path.
+ *
+ * This header is the drop-in boundary for the `loops` library's SpMV/SpMM
+ * hot path.  The reference exposes that path as C++ function templates with
+ * no ABI; each entry point below replaces one of them (file:line of the
+ * reference project in brackets):
+ *
+ *   el_spmv(.., EL_SCHED_THREAD_MAPPED, ..)
+ *       loops::algorithms::spmv::thread_mapped / original
+ *       [include/loops/algorithms/spmv/thread_mapped.cuh:68-91,
+ *        include/loops/algorithms/spmv/original.cuh:59-76]
+ *   el_spmv(.., EL_SCHED_GROUP_MAPPED, ..)
+ *       loops::algorithms::spmv::group_mapped
+ *       [include/loops/algorithms/spmv/group_mapped.cuh:73-105]
+ *   el_spmv(.., EL_SCHED_WORK_ORIENTED, ..)
+ *       loops::algorithms::spmv::work_oriented
+ *       [include/loops/algorithms/spmv/work_oriented.cuh:88-111]
+ *   el_spmv(.., EL_SCHED_MERGE_PATH_FLAT, ..)
+ *       loops::algorithms::spmv::merge_path_flat
+ *       [include/loops/algorithms/spmv/merge_path_flat.cuh:96-139]
+ *   el_spmm(..)
+ *       loops::algorithms::spmm::thread_mapped
+ *       [include/loops/algorithms/spmm/thread_mapped.cuh:67-90]
+ *   el_merge_path_partition / el_merge_path_thread_coords
+ *       loops::schedule::merge_path::generate_search_coordinates and
+ *       setup<merge_path_flat>::init
+ *       [include/loops/schedule/merge_path_flat.hxx:108-138, :321-385]
+ *   el_work_oriented_partition
+ *       setup<work_oriented>::init [include/loops/schedule/work_oriented.hxx:150-167]
+ *
+ * Conventions (differences from the reference are deliberate and listed):
+ *   - Every call is asynchronous on the given stream (the reference ends
+ *     each entry point with cudaStreamSynchronize).  Pointers are device
+ *     pointers on the current device.  Inputs are borrowed.
+ *   - y (or C) is OVERWRITTEN; it need not be zeroed first (the reference's
+ *     atomic schedules require a zeroed y; overwriting a zeroed y gives the
+ *     same result).
+ *   - No call throws across the ABI or exits the process; each returns an
+ *     el_status.  el_last_error_string() describes the last failure on the
+ *     calling thread.
+ *   - Kernels never read or write outside the arrays the el_csr describes,
+ *     whatever the offsets and indices contain: a malformed CSR gives wrong
+ *     numbers and sets a device error flag (read it with
+ *     el_workspace_errors), never a fault.  el_csr_validate checks a CSR
+ *     completely and synchronously.
+ *   - Values may be stored as FP32, BF16 or FP16; accumulation is always
+ *     FP32.  x and y are FP32.
+ */
+#ifndef EDGE_LOOPS_H_
+#define EDGE_LOOPS_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ABI-identical to cudaStream_t (NULL = the legacy default stream). */
+typedef struct CUstream_st* el_stream_t;
+
+#define EL_VERSION 100 /* 1.0.0 */
+
+typedef enum el_status {
+  EL_OK = 0,
+  EL_ERR_INVALID_ARGUMENT = 1, /* bad size, dtype, schedule option */
+  EL_ERR_NULL_POINTER = 2,     /* a required pointer is NULL */
+  EL_ERR_OVERFLOW = 3,         /* rows+nnz >= 2^31 (int32 merge path) */
+  EL_ERR_UNSUPPORTED = 4,      /* e.g. the reference's unimplemented
+                                  `bucketing` schedule */
+  EL_ERR_MALFORMED_CSR = 5,    /* el_csr_validate found a defect */
+  EL_ERR_CUDA = 6,             /* a CUDA runtime call failed */
+  EL_ERR_OUT_OF_MEMORY = 7,    /* workspace allocation failed */
+  EL_ERR_DEVICE = 8            /* a kernel reported an error flag */
+} el_status;
+
+/* Value storage types.  Accumulation is FP32 for all of them. */
+typedef enum el_dtype { EL_F32 = 0, EL_BF16 = 1, EL_F16 = 2 } el_dtype;
+
+/* Schedules.  Values 0-4 are the reference's
+ * loops::schedule::algorithms_t [include/loops/schedule.hxx:23-29]. */
+typedef enum el_schedule {
+  EL_SCHED_MERGE_PATH_FLAT = 0,
+  EL_SCHED_WORK_ORIENTED = 1,
+  EL_SCHED_THREAD_MAPPED = 2,
+  EL_SCHED_GROUP_MAPPED = 3,
+  EL_SCHED_BUCKETING = 4, /* declared by the reference, never implemented:
+                             returns EL_ERR_UNSUPPORTED */
+  EL_SCHED_AUTO = 5       /* new: pick by the built-in heuristic */
+} el_schedule;
+
+/* Device error flags (bit set), reported by el_workspace_errors and
+ * el_csr_validate. */
+#define EL_FLAG_INDEX_RANGE 0x1u  /* a column index outside [0, cols) */
+#define EL_FLAG_OFFSETS 0x2u      /* offsets not monotone / outside [0,nnz] */
+#define EL_FLAG_NNZ_MISMATCH 0x4u /* offsets[0] != 0 or offsets[rows] != nnz */
+#define EL_FLAG_TIMEOUT 0x8u      /* a bounded device wait ran out */
+
+/* A CSR matrix [include/loops/container/csr.hxx:32-95] as borrowed device
+ * pointers.  With row_scale != NULL, A[i][j] = row_scale[i] * values[ij]
+ * (per-row scales let BF16/FP16 storage keep each row in range; powers of
+ * two keep the product exact). */
+typedef struct el_csr {
+  int64_t rows;
+  int64_t cols;
+  int64_t nnz;
+  const int32_t* offsets; /* rows + 1 */
+  const int32_t* indices; /* nnz column indices */
+  const void* values;     /* nnz values of value_dtype */
+  int32_t value_dtype;    /* el_dtype */
+  int32_t reserved0;
+  const float* row_scale; /* rows, or NULL */
+} el_csr;
+
+/* Tuning knobs; zero means "the schedule's default".  Initialise with
+ * el_spmv_opts_default. */
+typedef struct el_spmv_opts {
+  int32_t threads_per_block; /* thread/group_mapped block size */
+  int32_t items_per_thread;  /* merge_path: merge items per thread and tile
+                                (1..16, tile = 256 x this); work_oriented:
+                                unused (even share per thread) */
+  int32_t threads_per_row;   /* thread_mapped: 1,2,4,8,16,32 lanes per row */
+  int32_t group_rows;        /* group_mapped: rows per group: 32 (one warp
+                                per group, the reference's warp_mapped) or
+                                threads_per_block (block_mapped) */
+  int64_t num_threads;       /* work_oriented: threads of the even split
+                                (the reference uses 2 x SMs x 128); 0 =
+                                resident capacity */
+  int32_t compensated;       /* 1: Neumaier / two-sum compensated FP32 sums */
+  int32_t max_ctas;          /* cap on persistent grids (0 = resident) */
+  int32_t wait_limit_us;     /* bound on every device-side wait (0 = 2 s) */
+  int32_t test_hooks;        /* testing only, 0 in normal use: bit 0 makes
+                                merge_path ranges skip publishing their row
+                                carries, so a range that needs one waits until
+                                wait_limit_us and reports EL_FLAG_TIMEOUT */
+  int32_t reserved[6];
+} el_spmv_opts;
+
+typedef struct el_workspace el_workspace;
+
+/* ---- library ---------------------------------------------------------- */
+int el_version(void);
+const char* el_status_string(el_status s);
+const char* el_last_error_string(void);
+void el_spmv_opts_default(el_spmv_opts* opts);
+
+/* ---- workspaces --------------------------------------------------------
+ * A workspace holds the small device state of the persistent schedules
+ * (tile tickets, cross-CTA carries, the error flags).  Calls that pass
+ * ws == NULL use a library-owned workspace per (device, stream).  A
+ * workspace must not be used by two streams at the same time. */
+el_status el_workspace_create(int device, el_workspace** out);
+el_status el_workspace_destroy(el_workspace* ws);
+/* Synchronises `stream`, returns the device error flags of `ws` (or of the
+ * library workspace of this device/stream when ws == NULL) and clears them
+ * when clear != 0. */
+el_status el_workspace_errors(el_workspace* ws, el_stream_t stream,
+                              uint32_t* flags, int clear);
+
+/* ---- SpMV / SpMM ------------------------------------------------------ */
+/* y = A x.  x has A->cols floats, y has A->rows floats. */
+el_status el_spmv(el_workspace* ws, const el_csr* A, int32_t schedule,
+                  const el_spmv_opts* opts, const float* x, float* y,
+                  el_stream_t stream);
+
+/* C = A B.  B is row-major A->cols x n (leading dimension ldb >= n) of
+ * b_dtype (FP32 / BF16 / FP16); C is row-major FP32 A->rows x n (ldc >= n).
+ * Schedules: THREAD_MAPPED (the reference's), GROUP_MAPPED (a warp per
+ * row, lanes across columns) and MERGE_PATH_FLAT. */
+el_status el_spmm(el_workspace* ws, const el_csr* A, int32_t schedule,
+                  const el_spmv_opts* opts, const void* B, int32_t b_dtype,
+                  int64_t n, int64_t ldb, float* C, int64_t ldc,
+                  el_stream_t stream);
+
+/* Checks offsets[0] == 0, offsets monotone, offsets[rows] == nnz and every
+ * index in [0, cols).  Synchronous.  *flags gets the EL_FLAG_* bits found;
+ * returns EL_ERR_MALFORMED_CSR when any is set. */
+el_status el_csr_validate(const el_csr* A, el_stream_t stream,
+                          uint32_t* flags);
+
+/* ---- partitions (exposed so split points can be checked bit for bit) --
+ * Number of merge tiles of tpb * ipt items over rows + nnz items. */
+int64_t el_merge_path_num_tiles(int64_t rows, int64_t nnz, int32_t tpb,
+                                int32_t ipt);
+/* Start coordinate (row, nonzero) of every merge tile plus the end of the
+ * last one: 2 * (num_tiles + 1) uint32 in device memory. */
+el_status el_merge_path_partition(const int32_t* offsets, int64_t rows,
+                                  int64_t nnz, int32_t tpb, int32_t ipt,
+                                  uint32_t* coords, el_stream_t stream);
+/* For every tile and thread, the tile-local coordinate the thread starts
+ * its items_per_thread steps from: 2 * num_tiles * tpb uint32. */
+el_status el_merge_path_thread_coords(const int32_t* offsets, int64_t rows,
+                                      int64_t nnz, int32_t tpb, int32_t ipt,
+                                      uint32_t* coords, el_stream_t stream);
+/* work_oriented even share over num_threads threads: per thread the start
+ * and end coordinate, 4 * num_threads int64 (st.row, st.nz, en.row, en.nz). */
+el_status el_work_oriented_partition(const int32_t* offsets, int64_t rows,
+                                     int64_t nnz, int64_t num_threads,
+                                     int64_t* coords, el_stream_t stream);
+
+/* ---- mixed precision -------------------------------------------------- */
+/* Converts FP32 values to BF16 / FP16 (round to nearest even).  With
+ * row_scale != NULL, each row is first divided by a power of two chosen so
+ * that the row's largest magnitude lands in [1, 2) and the power is written
+ * to row_scale[row] (exact: dequantised = out * row_scale). */
+el_status el_quantize_values(const int32_t* offsets, int64_t rows,
+                             int64_t nnz, const float* values, int32_t dtype,
+                             void* out_values, float* row_scale,
+                             el_stream_t stream);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* EDGE_LOOPS_H_ */

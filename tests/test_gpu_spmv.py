@@ -1,0 +1,248 @@
+"""GPU parity of the SpMV path against the oracle, through the C ABI.
+
+Bars: split points bit-identical to the restated reference search; the
+TPR=1 thread_mapped schedule bit-identical to the reference CPU loop; every
+schedule within the order-free FP32 bound gamma_(n+2) * sum|a x| of the FP64
+oracle (valid for any summation order) and within the reference's own
+|gpu - cpu| <= 1e-2 check."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import load_golden, order_free_bound, random_csr
+
+pytestmark = pytest.mark.gpu
+
+SCHEDS = [
+    ("merge_path_flat", {}),
+    ("merge_path_flat", {"items_per_thread": 4}),
+    ("merge_path_flat", {"compensated": True}),
+    ("work_oriented", {}),
+    ("thread_mapped", {}),
+    ("thread_mapped", {"threads_per_row": 8}),
+    ("thread_mapped", {"threads_per_row": 32}),
+    ("group_mapped", {}),
+    ("group_mapped", {"group_rows": 32}),
+    ("group_mapped", {"threads_per_block": 256, "group_rows": 256}),
+]
+IDS = [f"{s}{'-' + '-'.join(f'{k}{v}' for k, v in o.items()) if o else ''}" for s, o in SCHEDS]
+
+
+def dev_csr(off, idx, vals, cols, cuda):
+    from edge_loops_gb300.api import CSR
+    return CSR.from_arrays(off, idx, vals, cols, device=cuda)
+
+
+def run(A, x, sched, opts, cuda, fill=np.nan):
+    from edge_loops_gb300 import api
+    xt = torch.as_tensor(x, device=cuda)
+    y = torch.full((A.rows,), fill, dtype=torch.float32, device=cuda)
+    api.spmv(A, xt, y, schedule=sched, **opts)
+    flags = api.workspace_errors()
+    torch.cuda.synchronize()
+    return y.cpu().numpy(), flags
+
+
+def check_against_oracle(oracle_mod, off, idx, vals, x, y, scale=None):
+    y64, yabs = oracle_mod.spmv_f64(off, idx, vals, x, row_scale=scale)
+    bound = order_free_bound(off, yabs)
+    err = np.abs(y.astype(np.float64) - y64)
+    bad = np.nonzero(err > bound)[0]
+    assert len(bad) == 0, f"{len(bad)} rows off, first {bad[:5]} err {err[bad[:5]]} " \
+                          f"bound {bound[bad[:5]]}"
+    return oracle_mod.error_metrics(y, y64, yabs)
+
+
+@pytest.mark.parametrize("sched,opts", SCHEDS, ids=IDS)
+def test_chesapeake_exact(cuda, oracle_mod, sched, opts):
+    g = load_golden("chesapeake.npz")
+    A = dev_csr(g["offsets"], g["indices"], g["values"], int(g["cols"]), cuda)
+    y, flags = run(A, g["x"], sched, opts, cuda)
+    assert flags == 0
+    np.testing.assert_array_equal(y, g["y_exact"].astype(np.float32))
+
+
+@pytest.mark.parametrize("sched,opts", SCHEDS, ids=IDS)
+def test_uniform_1000_matches_reference_cpu(cuda, oracle_mod, sched, opts):
+    from edge_loops_gb300 import synth
+    off, idx, vals, x, cols = [t.numpy() if hasattr(t, "numpy") else t
+                               for t in synth.uniform_rows(seed=0)]
+    A = dev_csr(off, idx, vals, cols, cuda)
+    y, flags = run(A, x, sched, opts, cuda)
+    assert flags == 0
+    yref = oracle_mod.spmv_f32(off, idx, vals, x)
+    # the reference's validation (examples/spmv/helpers.hxx:138)
+    assert int(np.sum(np.abs(y - yref) > 1e-2)) == 0
+    check_against_oracle(oracle_mod, off, idx, vals, x, y)
+
+
+def test_thread_mapped_bit_exact_with_reference_loop(cuda, oracle_mod):
+    rng = np.random.default_rng(21)
+    off, idx, vals, x = random_csr(rng, rows=5000, cols=3000, max_len=60, empty_frac=0.1)
+    A = dev_csr(off, idx, vals, 3000, cuda)
+    y, _ = run(A, x, "thread_mapped", {}, cuda)
+    np.testing.assert_array_equal(y, oracle_mod.spmv_f32(off, idx, vals, x))
+
+
+def _power_law_case(cuda, rows=1 << 16, nnz=1_500_000, cap=40_000, seed=1):
+    from edge_loops_gb300 import synth
+    off, idx, vals, x, cols = synth.power_law(rows=rows, target_nnz=nnz, cap=cap, seed=seed)
+    return off.numpy(), idx.numpy(), vals.numpy(), x.numpy(), cols
+
+
+@pytest.mark.parametrize("sched,opts", SCHEDS, ids=IDS)
+def test_power_law_all_schedules(cuda, oracle_mod, sched, opts):
+    off, idx, vals, x, cols = _power_law_case(cuda)
+    A = dev_csr(off, idx, vals, cols, cuda)
+    y, flags = run(A, x, sched, opts, cuda)
+    assert flags == 0
+    check_against_oracle(oracle_mod, off, idx, vals, x, y)
+
+
+@pytest.mark.parametrize("sched,opts", SCHEDS, ids=IDS)
+def test_edge_cases(cuda, oracle_mod, sched, opts):
+    rng = np.random.default_rng(7)
+    cases = [
+        random_csr(rng, rows=1, cols=50000, max_len=0, long_rows=[(0, 40000)]),  # one long row
+        random_csr(rng, rows=3000, cols=100, max_len=5, empty_frac=0.9),  # mostly empty
+        random_csr(rng, rows=777, cols=1000, max_len=0, long_rows=[(3, 900), (776, 1000)]),
+        (np.zeros(101, dtype=np.int32), np.zeros(0, dtype=np.int32),
+         np.zeros(0, dtype=np.float32), np.ones(5, dtype=np.float32)),  # no nonzeros
+        random_csr(rng, rows=2, cols=3, max_len=3),
+    ]
+    for off, idx, vals, x in cases:
+        A = dev_csr(off, idx, vals, len(x), cuda)
+        y, flags = run(A, x, sched, opts, cuda)
+        assert flags == 0
+        check_against_oracle(oracle_mod, off, idx, vals, x, y)
+
+
+def test_long_rows_across_many_ctas(cuda, oracle_mod):
+    """Rows much longer than a CTA's range: the cross-range carry chain."""
+    rng = np.random.default_rng(13)
+    off, idx, vals, x = random_csr(rng, rows=400, cols=300_000, max_len=50,
+                                   long_rows=[(0, 250_000), (17, 120_000), (399, 200_000)])
+    A = dev_csr(off, idx, vals, 300_000, cuda)
+    for opts in ({"items_per_thread": 4}, {"items_per_thread": 4, "max_ctas": 7},
+                 {"max_ctas": 1}, {"compensated": True}):
+        y, flags = run(A, x, "merge_path_flat", opts, cuda)
+        assert flags == 0
+        check_against_oracle(oracle_mod, off, idx, vals, x, y)
+    for nt in (128, 128 * 64, 128 * 1000):
+        y, flags = run(A, x, "work_oriented", {"num_threads": nt}, cuda)
+        assert flags == 0
+        check_against_oracle(oracle_mod, off, idx, vals, x, y)
+
+
+@pytest.mark.parametrize("sched,opts", SCHEDS, ids=IDS)
+def test_deterministic(cuda, sched, opts):
+    off, idx, vals, x, cols = _power_law_case(cuda, rows=1 << 14, nnz=300_000, cap=20_000)
+    A = dev_csr(off, idx, vals, cols, cuda)
+    y1, _ = run(A, x, sched, opts, cuda)
+    y2, _ = run(A, x, sched, opts, cuda, fill=0.0)
+    np.testing.assert_array_equal(y1, y2)
+
+
+def test_merge_path_partition_bit_exact(cuda, oracle_mod):
+    from edge_loops_gb300 import api
+    for off, nnz in [(load_golden("chesapeake.npz")["offsets"], 340)] + \
+            [(_power_law_case(cuda, rows=5000, nnz=80_000, cap=9000)[0], None)]:
+        nnz = int(off[-1])
+        rows = len(off) - 1
+        d = torch.as_tensor(off, device=cuda)
+        for tpb, ipt in ((128, 5), (64, 3), (256, 8)):
+            got = api.merge_path_partition(d, rows, nnz, tpb, ipt).cpu().numpy().view(np.uint32)
+            exp = oracle_mod.merge_path_tile_coords(off, nnz, tpb * ipt)
+            np.testing.assert_array_equal(got, exp)
+            got = api.merge_path_thread_coords(d, rows, nnz, tpb, ipt).cpu().numpy()
+            exp = oracle_mod.merge_path_thread_coords(off, nnz, tpb, ipt)
+            np.testing.assert_array_equal(got.view(np.uint32), exp)
+        for nt in (128, 304 * 128, 1000):
+            got = api.work_oriented_partition(d, rows, nnz, nt).cpu().numpy()
+            np.testing.assert_array_equal(got, oracle_mod.work_oriented_coords(off, nnz, nt))
+
+
+def test_malformed_csr_sets_flags_without_fault(cuda, oracle_mod):
+    from edge_loops_gb300 import api
+    rng = np.random.default_rng(2)
+    off, idx, vals, x = random_csr(rng, rows=500, cols=100, max_len=20)
+    bad_idx = idx.copy()
+    bad_idx[::7] = 100 + 5  # outside [0, cols)
+    bad_idx[3] = -4
+    A = dev_csr(off, bad_idx, vals, 100, cuda)
+    assert api.validate(A) & 0x1
+    for sched, opts in SCHEDS:
+        y, flags = run(A, x, sched, opts, cuda)
+        assert flags & 0x1, sched
+    bad_off = off.copy()
+    bad_off[100] = bad_off[300]  # not monotone
+    bad_off[200] = -50
+    A = dev_csr(bad_off, idx, vals, 100, cuda)
+    assert api.validate(A) & 0x2
+    for sched, opts in SCHEDS:
+        y, flags = run(A, x, sched, opts, cuda)
+    short = off.copy()
+    short[-1] = off[-1] - 3  # offsets[rows] != nnz
+    A = dev_csr(short, idx, vals, 100, cuda)
+    assert api.validate(A) & 0x4
+    # the workspace is healthy afterwards
+    A = dev_csr(off, idx, vals, 100, cuda)
+    for sched, opts in SCHEDS:
+        y, flags = run(A, x, sched, opts, cuda)
+        assert flags == 0
+        check_against_oracle(oracle_mod, off, idx, vals, x, y)
+
+
+@pytest.mark.parametrize("dtype", [torch.bfloat16, torch.float16])
+@pytest.mark.parametrize("per_row", [True, False])
+def test_mixed_precision_stencil(cuda, oracle_mod, dtype, per_row):
+    from edge_loops_gb300 import api, synth
+    off, idx, vals, x, rows = [t.numpy() if hasattr(t, "numpy") else t
+                               for t in synth.stencil27(n=24, seed=2)]
+    A = dev_csr(off, idx, vals, rows, cuda)
+    Aq = A.quantized(dtype, per_row_scale=per_row)
+    qv = Aq.values.float().cpu().numpy()
+    sc = Aq.row_scale.cpu().numpy() if per_row else None
+    if per_row:
+        assert np.all(np.log2(sc) == np.round(np.log2(sc)))  # powers of two
+        row_of = np.repeat(np.arange(rows), np.diff(off))
+        assert np.all(np.abs(qv) < 2.0)
+        deq = qv * sc[row_of]
+    else:
+        deq = qv
+    u = 2.0 ** -8 if dtype == torch.bfloat16 else 2.0 ** -11
+    np.testing.assert_allclose(deq, vals, rtol=u, atol=0)
+    for sched, opts in SCHEDS:
+        y, flags = run(Aq, x, sched, opts, cuda)
+        assert flags == 0
+        # exact stored values: order-free bound against FP64 of the stored matrix
+        check_against_oracle(oracle_mod, off, idx, qv, x, y, scale=sc)
+        # against the FP32 matrix: the quantisation error is inside 1e-2
+        y64, yabs = oracle_mod.spmv_f64(off, idx, vals, x)
+        comp, _ = oracle_mod.error_metrics(y, y64, yabs)
+        assert comp <= 1e-2, (sched, comp)
+
+
+def test_lookback_wait_times_out_with_status(cuda):
+    """A bounded device wait that nothing satisfies ends with a status
+    (EL_FLAG_TIMEOUT), not a hang; the workspace stays usable."""
+    from edge_loops_gb300 import api
+    rng = np.random.default_rng(8)
+    off, idx, vals, x = random_csr(rng, rows=10, cols=100_000, max_len=5,
+                                   long_rows=[(4, 90_000)])
+    A = dev_csr(off, idx, vals, 100_000, cuda)
+    ws = api.Workspace()
+    xt = torch.as_tensor(x, device=cuda)
+    y = torch.empty(A.rows, device=cuda)
+    o = api.make_opts(items_per_thread=4, wait_limit_us=2000)
+    o.test_hooks = 1  # ranges do not publish their carries
+    import ctypes as C
+    from edge_loops_gb300 import _lib
+    a = A.el()
+    st = _lib.lib().el_spmv(ws.handle, C.byref(a), 0, C.byref(o), C.c_void_p(xt.data_ptr()),
+                            C.c_void_p(y.data_ptr()),
+                            C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0
+    assert ws.errors() & 0x8
+    api.spmv(A, xt, y, workspace=ws, items_per_thread=4)
+    assert ws.errors() == 0
