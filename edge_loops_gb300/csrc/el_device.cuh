@@ -16,25 +16,46 @@ namespace el {
 constexpr unsigned kFullMask = 0xffffffffu;
 
 // ---------------------------------------------------------------- workspace
-// Device state of the persistent schedules.  Every kernel that uses it
-// leaves it exactly as it found it (tickets back to 0, every carry flag it
-// published consumed and cleared), so a launch can be replayed from a CUDA
-// graph without any host-side bookkeeping.
+// Device state of the persistent schedules.  A launch reads `epoch` when it
+// starts and tags every carry it publishes with epoch_tag(epoch); readers
+// accept only that tag, so carries left by any earlier launch are never
+// mistaken for fresh ones.  The last CTA (or warp) of a launch resets the
+// ticket and done counters and advances the epoch, all on the device, so a
+// launch can be replayed from a CUDA graph without host-side bookkeeping.
 struct WsHeader {
   unsigned int ticket;    // next range/tile id handed out
   unsigned int done;      // CTAs finished (the last one resets both)
   unsigned int errors;    // EL_FLAG_* bits, sticky until cleared
   unsigned int err_info;  // first offending index (diagnostics)
-  unsigned int pad[12];
+  unsigned int epoch;     // launches completed on this workspace
+  unsigned int pad[11];
 };
 static_assert(sizeof(WsHeader) == 64, "header is one 64-byte line");
 
 struct CarrySlot {  // one partial row sum handed to a later CTA
   float sum;
   float comp;
-  unsigned int flag;  // 1 = published, consumed (reset to 0) by the reader
+  unsigned int flag;  // == epoch_tag(epoch of the publishing launch)
   unsigned int pad;
 };
+
+// Never 0 (the value of a slot nobody ever published).
+__device__ __forceinline__ unsigned epoch_tag(unsigned epoch) {
+  return epoch + 1u == 0u ? 1u : epoch + 1u;
+}
+
+__device__ __forceinline__ unsigned read_epoch(const WsHeader* h) {
+  return *reinterpret_cast<const volatile unsigned*>(&h->epoch);
+}
+
+// Called by the last CTA/warp of a launch: hand the counters back and
+// advance the epoch for the next launch on this workspace.
+__device__ __forceinline__ void finish_launch(WsHeader* h, unsigned epoch) {
+  atomicExch(&h->ticket, 0u);
+  atomicExch(&h->done, 0u);
+  atomicExch(&h->epoch, epoch + 1u);
+  __threadfence();
+}
 
 struct WsView {
   WsHeader* hdr;

@@ -150,9 +150,14 @@ __global__ void __launch_bounds__(256) merge_path_kernel(const MpArgs m) {
   const VT* vals = reinterpret_cast<const VT*>(a.values);
   const BT* B = reinterpret_cast<const BT*>(a.B);
   const int lane = threadIdx.x & 31;
-  unsigned wt = 0;
-  if (lane == 0) wt = atomicAdd(&a.hdr->ticket, 1u);
+  unsigned wt = 0, ep = 0;
+  if (lane == 0) {
+    wt = atomicAdd(&a.hdr->ticket, 1u);
+    ep = read_epoch(a.hdr);
+  }
   const long long w = __shfl_sync(kFullMask, wt, 0);
+  const unsigned epoch = __shfl_sync(kFullMask, ep, 0);
+  const unsigned tag = epoch_tag(epoch);
   const long long total = a.rows + a.nnz;
   if (w < m.num_ranges) {
     long long d0 = w * m.range_items, d1 = d0 + m.range_items;
@@ -221,7 +226,7 @@ __global__ void __launch_bounds__(256) merge_path_kernel(const MpArgs m) {
         }
         __threadfence();
         __syncwarp();
-        if (lane == 0) st_release_u32(&m.flags[w].flag, 1u);
+        if (lane == 0) st_release_u32(&m.flags[w].flag, tag);
       }
     }
     if (has_pend) {
@@ -232,14 +237,14 @@ __global__ void __launch_bounds__(256) merge_path_kernel(const MpArgs m) {
       bool ok = true;
       for (long long k2 = wfirst; k2 < w && ok; ++k2) {
         unsigned f = ld_acquire_u32(&m.flags[k2].flag);
-        if (f == 0u) {
+        if (f != tag) {
           const uint64_t t0 = global_timer_ns();
-          while ((f = ld_acquire_u32(&m.flags[k2].flag)) == 0u) {
+          while ((f = ld_acquire_u32(&m.flags[k2].flag)) != tag) {
             if (global_timer_ns() - t0 > m.wait_ns) break;
             __nanosleep(100);
           }
         }
-        ok = __all_sync(kFullMask, f != 0u);
+        ok = __all_sync(kFullMask, f == tag);
         if (!ok) break;
         const float* src = m.vec + k2 * 128;
 #pragma unroll
@@ -248,7 +253,6 @@ __global__ void __launch_bounds__(256) merge_path_kernel(const MpArgs m) {
           if (c < a.n) chain[k] = __fadd_rn(chain[k], __ldcg(src + c));
         }
         __syncwarp();
-        if (lane == 0) m.flags[k2].flag = 0u;
       }
       if (!ok && lane == 0) raise_flag(a.hdr, EL_FLAG_TIMEOUT, 6);
 #pragma unroll
@@ -261,11 +265,7 @@ __global__ void __launch_bounds__(256) merge_path_kernel(const MpArgs m) {
     __threadfence();
     const unsigned total_warps = gridDim.x * (blockDim.x >> 5);
     const unsigned prev = atomicAdd(&a.hdr->done, 1u);
-    if (prev == total_warps - 1) {
-      atomicExch(&a.hdr->ticket, 0u);
-      atomicExch(&a.hdr->done, 0u);
-      __threadfence();
-    }
+    if (prev == total_warps - 1) finish_launch(a.hdr, epoch);
   }
 }
 

@@ -84,6 +84,7 @@ template <int NW>
 struct Ctl {
   long long rs, ns, re, ne;  // range start / end coordinate (row, nonzero)
   int g;                     // range id
+  unsigned epoch;
   int abort;
   int pend;
   float pend_s, pend_c;
@@ -111,6 +112,7 @@ __global__ void __launch_bounds__(Cfg<IPT>::TPB)
 
   if (tid == 0) {
     ctl.g = (int)atomicAdd(&hdr->ticket, 1u);
+    ctl.epoch = read_epoch(hdr);
     ctl.abort = 0;
     ctl.pend = 0;
     for (int i = 0; i < K_O; ++i) {
@@ -125,6 +127,8 @@ __global__ void __launch_bounds__(Cfg<IPT>::TPB)
   }
   __syncthreads();
   const int g = ctl.g;
+  const unsigned epoch = ctl.epoch;
+  const unsigned tag = epoch_tag(epoch);
   const long long total = a.rows + a.nnz;
   const bool active = g < a.num_ranges;  // false only if the state was stale
   if (warp < 2) {
@@ -369,8 +373,10 @@ __global__ void __launch_bounds__(Cfg<IPT>::TPB)
       if (first_x >= 0) {
         Acc<COMP> v = ex.v;  // earlier parts of the row first
         v.add(first_v);
-        if (first_tile && first_x == 0 && need_lb) {
-          ctl.pend = 1;  // finished by the look-back below
+        if (need_lb && r0 + first_x == rs) {
+          // the range's first row end closes row rs, begun in an earlier
+          // range: finished by the look-back below
+          ctl.pend = 1;
           ctl.pend_s = v.s;
           ctl.pend_c = v.comp();
         } else {
@@ -412,20 +418,21 @@ __global__ void __launch_bounds__(Cfg<IPT>::TPB)
           CarrySlot* sl = a.ws.slots + g;
           sl->sum = carry.s;
           sl->comp = carry.comp();
-          st_release_u32(&sl->flag, 1u);
+          st_release_u32(&sl->flag, tag);
         }
       }
       if (warp == 0 && need_lb && ctl.pend) {
         // the row rs began in range gfirst: sum the partials of ranges
-        // [gfirst, g) in a fixed order
+        // [gfirst, g) in a fixed order (each published with this launch's
+        // tag; exactly this range reads them)
         const long long gfirst = (rs + off_rs) / a.range_items;
         Acc<COMP> acc;
         bool ok = true;
         for (long long k = gfirst + lane; k < g && k < a.ws.nslots; k += 32) {
           CarrySlot* sl = a.ws.slots + k;
-          if (ld_acquire_u32(&sl->flag) == 0u) {
+          if (ld_acquire_u32(&sl->flag) != tag) {
             const uint64_t t0 = global_timer_ns();
-            while (ld_acquire_u32(&sl->flag) == 0u) {
+            while (ld_acquire_u32(&sl->flag) != tag) {
               if (global_timer_ns() - t0 > a.wait_ns) {
                 ok = false;
                 break;
@@ -437,7 +444,6 @@ __global__ void __launch_bounds__(Cfg<IPT>::TPB)
           Acc<COMP> v;
           v.set(__ldcg(&sl->sum), __ldcg(&sl->comp));
           acc.add(v);
-          sl->flag = 0u;
         }
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) {
@@ -470,11 +476,7 @@ __global__ void __launch_bounds__(Cfg<IPT>::TPB)
   if (tid == 0) {
     __threadfence();
     const unsigned prev = atomicAdd(&hdr->done, 1u);
-    if (prev == gridDim.x - 1) {
-      atomicExch(&hdr->ticket, 0u);
-      atomicExch(&hdr->done, 0u);
-      __threadfence();
-    }
+    if (prev == gridDim.x - 1) finish_launch(hdr, epoch);
   }
 }
 

@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(TPB)
     const long long g = g0 + grp;
     const long long r0 = g * GT;
     const int glen = g < ngroups ? (int)((a.rows - r0 < GT) ? a.rows - r0 : GT) : 0;
-    for (int k = t; k <= glen; k += GT) {
+    for (int k = t; glen > 0 && k <= glen; k += GT) {
       long long v = __ldg(a.offsets + r0 + k);
       if (v < 0 || v > a.nnz) {
         raise_flag(a.hdr, EL_FLAG_OFFSETS, (unsigned)(r0 + k));
@@ -200,6 +200,7 @@ struct WoArgs {
 template <int NW>
 struct WoCtl {
   int blk;
+  unsigned epoch;
   int pend;
   float pend_s, pend_c;
   SegScratch<NW> scan;
@@ -213,10 +214,13 @@ __global__ void __launch_bounds__(TPB)
   const int lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     ctl.blk = (int)atomicAdd(&w.ws.hdr->ticket, 1u);
+    ctl.epoch = read_epoch(w.ws.hdr);
     ctl.pend = 0;
   }
   __syncthreads();
   const int blk = ctl.blk;
+  const unsigned epoch = ctl.epoch;
+  const unsigned tag = epoch_tag(epoch);
   const bool active = blk < w.num_blocks;
   const long long total = a.rows + a.nnz;
   const long long tid = (long long)blk * TPB + threadIdx.x;
@@ -289,7 +293,7 @@ __global__ void __launch_bounds__(TPB)
         CarrySlot* sl = w.ws.slots + blk;
         sl->sum = tot.v.s;
         sl->comp = tot.v.comp();
-        st_release_u32(&sl->flag, 1u);
+        st_release_u32(&sl->flag, tag);
       }
     }
   }
@@ -301,9 +305,9 @@ __global__ void __launch_bounds__(TPB)
     bool ok = true;
     for (long long k = gfirst + lane; k < blk && k < w.ws.nslots; k += 32) {
       CarrySlot* sl = w.ws.slots + k;
-      if (ld_acquire_u32(&sl->flag) == 0u) {
+      if (ld_acquire_u32(&sl->flag) != tag) {
         const uint64_t t0 = global_timer_ns();
-        while (ld_acquire_u32(&sl->flag) == 0u) {
+        while (ld_acquire_u32(&sl->flag) != tag) {
           if (global_timer_ns() - t0 > w.wait_ns) {
             ok = false;
             break;
@@ -315,7 +319,6 @@ __global__ void __launch_bounds__(TPB)
       Acc<COMP> v;
       v.set(__ldcg(&sl->sum), __ldcg(&sl->comp));
       acc.add(v);
-      sl->flag = 0u;
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
@@ -342,11 +345,7 @@ __global__ void __launch_bounds__(TPB)
   if (threadIdx.x == 0) {
     __threadfence();
     const unsigned prev = atomicAdd(&w.ws.hdr->done, 1u);
-    if (prev == gridDim.x - 1) {
-      atomicExch(&w.ws.hdr->ticket, 0u);
-      atomicExch(&w.ws.hdr->done, 0u);
-      __threadfence();
-    }
+    if (prev == gridDim.x - 1) finish_launch(w.ws.hdr, epoch);
   }
 }
 

@@ -165,9 +165,11 @@ el_status launch_validate(const el_csr& A, unsigned* d_flags, cudaStream_t s) {
 }
 
 // ----------------------------------------------------------- quantisation
-// One warp per row: with scales, the row's largest magnitude m picks
-// s = 2^floor(log2 m) so that |v / s| < 2 for every value, and the stored
-// value is round-to-nearest-even(v / s) (the division is exact).
+// One warp per row: with scales, the row's largest magnitude m picks a power
+// of two s so that m / s lands in [2^top, 2^(top+1)) and the stored value is
+// round-to-nearest-even(v / s) (the division by s is exact).  BF16 has
+// FP32's exponent range, so top = 0; FP16 tops out at 65504 and goes
+// subnormal below 2^-14, so top = 14 keeps the most of each row normal.
 template <typename OT>
 __device__ __forceinline__ OT from_f32(float v);
 template <>
@@ -178,6 +180,10 @@ template <>
 __device__ __forceinline__ __half from_f32<__half>(float v) {
   return __float2half_rn(v);
 }
+
+template <typename OT> struct QTop;
+template <> struct QTop<__nv_bfloat16> { static constexpr int value = 0; };
+template <> struct QTop<__half> { static constexpr int value = 14; };
 
 template <typename OT>
 __global__ void quantize_kernel(const int* __restrict__ offsets, long long rows,
@@ -197,7 +203,7 @@ __global__ void quantize_kernel(const int* __restrict__ offsets, long long rows,
       if (m > 0.f && isfinite(m)) {
         const unsigned bits = __float_as_uint(m);
         const int be = (int)((bits >> 23) & 0xff);
-        ex = be == 0 ? -126 : be - 127;  // floor(log2 m) for normal m
+        ex = (be == 0 ? -126 : be - 127) - QTop<OT>::value;  // floor(log2 m) - top
       }
       if (lane == 0) scale[r] = ldexpf(1.f, ex);
     }

@@ -203,15 +203,21 @@ def test_mixed_precision_stencil(cuda, oracle_mod, dtype, per_row):
     Aq = A.quantized(dtype, per_row_scale=per_row)
     qv = Aq.values.float().cpu().numpy()
     sc = Aq.row_scale.cpu().numpy() if per_row else None
+    row_of = np.repeat(np.arange(rows), np.diff(off))
+    top = 0 if dtype == torch.bfloat16 else 14  # row max lands in [2^top, 2^(top+1))
     if per_row:
         assert np.all(np.log2(sc) == np.round(np.log2(sc)))  # powers of two
-        row_of = np.repeat(np.arange(rows), np.diff(off))
-        assert np.all(np.abs(qv) < 2.0)
-        deq = qv * sc[row_of]
+        assert np.all(np.abs(qv) < 2.0 ** (top + 1))
+        rmax = np.maximum.reduceat(np.abs(qv), off[:-1])
+        assert np.all(rmax >= 2.0 ** top)
+        s_of = sc[row_of]
     else:
-        deq = qv
-    u = 2.0 ** -8 if dtype == torch.bfloat16 else 2.0 ** -11
-    np.testing.assert_allclose(deq, vals, rtol=u, atol=0)
+        s_of = np.ones(len(qv))
+    deq = qv * s_of
+    u = 2.0 ** -9 if dtype == torch.bfloat16 else 2.0 ** -12  # half an ulp, relative
+    tiny = 0.0 if dtype == torch.bfloat16 else 2.0 ** -25  # half a subnormal ulp of FP16
+    err = np.abs(deq.astype(np.float64) - vals)
+    assert np.all(err <= np.maximum(u * np.abs(vals), tiny * s_of)), np.max(err)
     for sched, opts in SCHEDS:
         y, flags = run(Aq, x, sched, opts, cuda)
         assert flags == 0
