@@ -65,6 +65,28 @@ class ElSpmvOpts(C.Structure):
     ]
 
 
+class ElBatchItem(C.Structure):
+    _fields_ = [("A", ElCsr), ("x", C.c_void_p), ("y", C.c_void_p)]
+
+
+EL_BATCH_ROW_BUCKETS = 21
+EL_BATCH_LEN_BUCKETS = 11
+EL_BATCH_CV_BUCKETS = 4
+EL_BATCH_TABLE_SIZE = EL_BATCH_ROW_BUCKETS * EL_BATCH_LEN_BUCKETS * EL_BATCH_CV_BUCKETS
+EL_BATCH_MAX_ROW_NNZ = 16384
+
+
+class ElBatchOpts(C.Structure):
+    _fields_ = [
+        ("table", C.c_void_p),
+        ("use_graph", C.c_int32),
+        ("force_threads_per_row", C.c_int32),
+        ("force_chunk_log2", C.c_int32),
+        ("max_ctas", C.c_int32),
+        ("reserved", C.c_int32 * 8),
+    ]
+
+
 # name -> (restype, argtypes); every symbol include/edge_loops.h declares
 SIGNATURES = {
     "el_version": (C.c_int, []),
@@ -89,6 +111,15 @@ SIGNATURES = {
                                              C.c_void_p, C.c_void_p]),
     "el_quantize_values": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_int32,
                                      C.c_void_p, C.c_void_p, C.c_void_p]),
+    "el_batch_opts_default": (None, [C.POINTER(ElBatchOpts)]),
+    "el_batch_plan_create": (C.c_int, [C.POINTER(ElBatchItem), C.c_int32,
+                                       C.POINTER(ElBatchOpts), C.c_void_p,
+                                       C.POINTER(C.c_void_p)]),
+    "el_batch_plan_execute": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "el_batch_plan_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_int32)]),
+    "el_batch_plan_errors": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint32), C.c_int]),
+    "el_batch_plan_destroy": (C.c_int, [C.c_void_p]),
 }
 
 _lib = None

@@ -96,7 +96,8 @@ class CSR:
 
     def quantized(self, dtype, per_row_scale=True, stream=None):
         """BF16/FP16 copy of an FP32 matrix (el_quantize_values); with
-        per_row_scale each row is scaled by a power of two into [1, 2)."""
+        per_row_scale each row is divided by a power of two that puts its
+        largest magnitude in [1, 2) (BF16) or [2^14, 2^15) (FP16)."""
         if self.values.dtype != torch.float32:
             raise TypeError("quantize an FP32 matrix")
         out = torch.empty(self.nnz, dtype=dtype, device=self.device)
@@ -231,3 +232,105 @@ def work_oriented_partition(offsets, rows, nnz, num_threads, stream=None):
                                                _ptr(out), _stream(stream)),
             "el_work_oriented_partition")
     return out.view(num_threads, 4)
+
+
+# ---------------------------------------------------------------- batched SpMV
+def load_tuning_table(path=None):
+    """The batched tuning table (int32[EL_BATCH_TABLE_SIZE]) from the JSON the
+    tuner wrote (edge_loops_gb300/batch_tuning.json by default), or None."""
+    import json
+    import os
+    import numpy as np
+    path = path or os.path.join(os.path.dirname(os.path.abspath(__file__)), "batch_tuning.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    t = np.zeros(L.EL_BATCH_TABLE_SIZE, dtype=np.int32)
+    for key, (tpr, chunk_log2) in d["entries"].items():
+        rb, lb, cb = (int(v) for v in key.split(","))
+        idx = (rb * L.EL_BATCH_LEN_BUCKETS + lb) * L.EL_BATCH_CV_BUCKETS + cb
+        t[idx] = int(tpr) | (int(chunk_log2) << 8)
+    return t
+
+
+class BatchPlan:
+    """el_batch_plan: y_i = A_i x_i for many independent matrices in one
+    persistent launch captured in a CUDA graph.  `items` is a list of
+    (CSR, x, y); the tensors must stay alive (the plan keeps references)."""
+
+    def __init__(self, items, table="default", use_graph=True, force_threads_per_row=0,
+                 force_chunk_log2=0, max_ctas=0, stream=None):
+        import numpy as np
+        self._keep = list(items)
+        arr = (L.ElBatchItem * max(len(items), 1))()
+        for i, (A, x, y) in enumerate(items):
+            arr[i].A = A.el()
+            arr[i].x = x.data_ptr() if x is not None and x.numel() else None
+            arr[i].y = y.data_ptr() if y is not None and y.numel() else None
+        o = L.ElBatchOpts()
+        L.lib().el_batch_opts_default(C.byref(o))
+        if isinstance(table, str) and table == "default":
+            table = load_tuning_table()
+        self._table = None if table is None else np.ascontiguousarray(table, dtype=np.int32)
+        o.table = self._table.ctypes.data if self._table is not None else None
+        o.use_graph = int(bool(use_graph))
+        o.force_threads_per_row = force_threads_per_row
+        o.force_chunk_log2 = force_chunk_log2
+        o.max_ctas = max_ctas
+        h = C.c_void_p()
+        L.check(L.lib().el_batch_plan_create(arr, len(items), C.byref(o), _stream(stream),
+                                             C.byref(h)), "el_batch_plan_create")
+        self.handle = h
+
+    def execute(self, stream=None):
+        L.check(L.lib().el_batch_plan_execute(self.handle, _stream(stream)),
+                "el_batch_plan_execute")
+
+    def info(self):
+        w = C.c_int64()
+        t = (C.c_int32 * 6)()
+        hv = C.c_int32()
+        L.check(L.lib().el_batch_plan_info(self.handle, C.byref(w), t, C.byref(hv)),
+                "el_batch_plan_info")
+        return {"work_items": int(w.value),
+                "matrices_by_threads_per_row": {1 << i: int(t[i]) for i in range(6)},
+                "heavy_matrices": int(hv.value)}
+
+    def errors(self, clear=True, stream=None):
+        f = C.c_uint32(0)
+        L.check(L.lib().el_batch_plan_errors(self.handle, _stream(stream), C.byref(f),
+                                             int(clear)), "el_batch_plan_errors")
+        return int(f.value)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            L.lib().el_batch_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batched_items(rows, off_cat, idx, vals, x_cat, row_start, nz_start, y_cat=None,
+                  row_scale_cat=None):
+    """CSR views of the concatenated arrays synth.batched returns: a list of
+    (CSR, x, y) with y slices of y_cat (allocated if None)."""
+    dev = off_cat.device
+    if y_cat is None:
+        y_cat = torch.empty(x_cat.numel(), dtype=torch.float32, device=dev)
+    rows_l = rows.tolist()
+    rs_l = row_start.tolist()
+    ns_l = nz_start.tolist()
+    out = []
+    for m, r in enumerate(rows_l):
+        o = off_cat[rs_l[m] + m: rs_l[m] + m + r + 1]
+        nnz = int(o[-1]) if r else 0
+        A = CSR(o, idx[ns_l[m]: ns_l[m] + nnz], vals[ns_l[m]: ns_l[m] + nnz], r, r,
+                row_scale=None if row_scale_cat is None else
+                row_scale_cat[rs_l[m]: rs_l[m] + r])
+        out.append((A, x_cat[rs_l[m]: rs_l[m] + r], y_cat[rs_l[m]: rs_l[m] + r]))
+    return out, y_cat

@@ -194,6 +194,24 @@ el_status resolve_ws(el_workspace* ws, cudaStream_t stream, int device,
 }
 
 }  // namespace
+
+WsView workspace_view(el_workspace* ws) { return ws_view(ws); }
+
+el_status workspace_prepare(el_workspace* ws, const el_csr& A, int schedule) {
+  SpmvCall c;
+  c.A = A;
+  c.x = nullptr;
+  c.y = nullptr;
+  el_spmv_opts_default(&c.o);
+  c.stream = nullptr;
+  c.wait_ns = kDefaultWaitNs;
+  c.device = ws->device;
+  c.ws = ws_view(ws);
+  if (schedule == EL_SCHED_MERGE_PATH_FLAT) return ws_reserve(ws, merge_path_slots_needed(c));
+  if (schedule == EL_SCHED_WORK_ORIENTED) return ws_reserve(ws, work_oriented_slots_needed(c));
+  return EL_OK;
+}
+
 }  // namespace el
 
 using namespace el;

@@ -209,6 +209,42 @@ __device__ __forceinline__ void named_bar_sync(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
+// The same barrier, also returning the OR of `v` over the participants.
+__device__ __forceinline__ bool named_bar_or(int id, int nthreads, bool v) {
+  int r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.s32 q, %1, 0;\n\t"
+      "bar.red.or.pred p, %2, %3, q;\n\t"
+      "selp.s32 %0, 1, 0, p;\n\t}"
+      : "=r"(r)
+      : "r"((int)v), "r"(id), "r"(nthreads)
+      : "memory");
+  return r != 0;
+}
+
+// First k in [lo, hi) where pred(k) is false, pred being true on a prefix
+// (else hi): 33-ary search by the whole warp, each round testing 32 evenly
+// spaced candidates, so a range of 2048 takes three rounds.  All 32 lanes
+// call it and get the same answer; the answer stays in [lo, hi] whatever
+// pred returns.
+template <typename Pred>
+__device__ __forceinline__ int warp_lower_bound(int lo, int hi, const Pred& pred) {
+  const int lane = threadIdx.x & 31;
+  while (hi - lo > 32) {
+    const int span = hi - lo;
+    const int p = lo + ((lane + 1) * span) / 33;
+    const int c = __popc(__ballot_sync(kFullMask, pred(p)));
+    const int plo = __shfl_sync(kFullMask, p, c > 0 ? c - 1 : 0);
+    const int phi = __shfl_sync(kFullMask, p, c < 32 ? c : 31);
+    if (c > 0) lo = plo + 1;
+    if (c < 32) hi = phi;
+  }
+  const int p = lo + lane;
+  const bool t = (p < hi) && pred(p);
+  return lo + __popc(__ballot_sync(kFullMask, t));
+}
+
 // ------------------------------------------------------------ merge path
 // Merge of the row-end offsets (list a) with the nonzero indices (list b,
 // a counting sequence) cut at a diagonal: the reference's

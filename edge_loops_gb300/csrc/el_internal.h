@@ -74,6 +74,11 @@ el_status launch_spmm(const SpmmCall& c, int schedule);
 size_t spmm_scratch_bytes(const SpmmCall& c, int schedule);
 long long spmm_slots_needed(const SpmmCall& c, int schedule);
 
+// Workspace internals for other translation units of the library.
+WsView workspace_view(el_workspace* ws);
+// Sizes `ws` for an SpMV of A with `schedule` (default options).
+el_status workspace_prepare(el_workspace* ws, const el_csr& A, int schedule);
+
 el_status launch_partition_tiles(const int32_t* offsets, int64_t rows,
                                  int64_t nnz, int64_t items,
                                  uint32_t* coords, cudaStream_t s);

@@ -5,10 +5,10 @@
 // [include/loops/schedule/merge_path_flat.hxx:244-436,
 //  include/loops/algorithms/spmv/merge_path_flat.cuh:38-139]: the merge of
 // the row-end offsets with the nonzero indices is cut into tiles of
-// ITEMS = 256 * IPT merge items at global diagonals k * ITEMS, and every
-// thread of a tile starts at the split point of local diagonal
-// tid * IPT, found by the same search (util/search.hxx:34-60).  What differs
-// is how the tiles are fed and stitched:
+// ITEMS = 256 * IPT merge items at global diagonals k * ITEMS, and thread t
+// of a tile starts at the split point of local diagonal t * IPT (the split
+// the reference finds with util/search.hxx:34-60).  What differs is how the
+// tiles are fed, split and stitched:
 //
 //   * one CTA per resident slot takes a contiguous RANGE of tiles (its id
 //     comes from an atomic ticket, so every range it may wait on is already
@@ -16,13 +16,17 @@
 //     the reference's two binary searches per tile;
 //   * two producer warps stream the range's row offsets and its
 //     (column, value) pairs into shared-memory rings with 1-D bulk copies
-//     (cp.async.bulk, mbarrier completion, L2 evict-first), so the eight
-//     consumer warps never wait on HBM latency for the matrix itself;
-//   * consumers gather x, form the products once per nonzero, walk their
-//     IPT items in shared memory and stitch rows that cross threads with a
-//     block-wide segmented scan, and rows that cross tiles through a
-//     register carry, instead of one atomicAdd per nonzero (the reference's
-//     merge_path_flat.cuh:77);
+//     (cp.async.bulk, mbarrier completion, L2 evict-first), several tiles
+//     ahead of the eight consumer warps;
+//   * per tile, each consumer warp finds the tile end with a 33-ary search
+//     in shared memory, and the threads' split points are SCATTERED from the
+//     row ends (row end k at merge position p_k closes the rows of every
+//     thread whose diagonal lies beyond p_k) instead of searched: the same
+//     split points, without a binary search per thread;
+//   * consumers gather x and form every product once, walk their IPT items
+//     in shared memory and stitch rows that cross threads with a block-wide
+//     segmented scan and rows that cross tiles through a register carry,
+//     instead of one atomicAdd per nonzero (merge_path_flat.cuh:77);
 //   * a row that crosses CTA ranges is finished by the range where it ends,
 //     which sums the carries the earlier ranges publish (bounded spins, in a
 //     fixed order: the result is deterministic).  y is overwritten.
@@ -42,10 +46,13 @@ struct Cfg {
   static constexpr int ITEMS = TPB_C * IPT;  // merge items per tile
   static constexpr int LOG_C = 9;
   static constexpr int C = 1 << LOG_C;  // elements per ring chunk
-  // A tile needs at most ITEMS+1 offsets and ITEMS nonzeros, which span at
-  // most ceil(ITEMS/C)+1 chunks; the rest of each ring is prefetch depth.
-  static constexpr int K_O = (ITEMS + C - 1) / C + 3;
-  static constexpr int K_N = (ITEMS + C - 1) / C + 4;
+  // A tile needs at most ITEMS+1 offsets and ITEMS nonzeros; starting
+  // anywhere in a chunk they span at most ITEMS/C + 2 chunks.  The rest of
+  // each ring is prefetch depth.
+  static constexpr int K_O = (ITEMS + 4 + C - 1) / C + 2;
+  static constexpr int K_N = ITEMS / C + 6;
+  static constexpr int RING_O = K_O * C;
+  static constexpr int RING_N = K_N * C;
   static constexpr int WARP_PO = NW_C;      // offsets producer warp
   static constexpr int WARP_PN = NW_C + 1;  // nonzero producer warp
 };
@@ -74,22 +81,24 @@ struct Smem {
   uint64_t empty_o[C_::K_O];
   uint64_t full_n[C_::K_N];
   uint64_t empty_n[C_::K_N];
-  alignas(16) int ring_o[C_::K_O * C_::C];
-  alignas(16) int ring_c[C_::K_N * C_::C];
-  alignas(16) VT ring_v[C_::K_N * C_::C];
-  alignas(16) float prod[C_::ITEMS];
+  alignas(16) int ring_o[C_::RING_O];
+  alignas(16) int ring_c[C_::RING_N];
+  alignas(16) VT ring_v[C_::RING_N];
+  alignas(16) float prod[2][C_::ITEMS];  // per tile parity
+  int sx[2][C_::TPB_C + 1];              // first row of every thread
 };
 
 template <int NW>
 struct Ctl {
-  long long rs, ns, re, ne;  // range start / end coordinate (row, nonzero)
-  int g;                     // range id
+  int rs, ns, re, ne;  // range start / end coordinate (row, nonzero)
+  int g;               // range id
   unsigned epoch;
-  int abort;
   int pend;
   float pend_s, pend_c;
   SegScratch<NW> scan;
 };
+
+__device__ __forceinline__ int wrap(int q, int ring) { return q >= ring ? q - ring : q; }
 
 template <typename VT, int IPT, bool COMP>
 __global__ void __launch_bounds__(Cfg<IPT>::TPB)
@@ -100,6 +109,8 @@ __global__ void __launch_bounds__(Cfg<IPT>::TPB)
   constexpr int K_N = C_::K_N;
   constexpr int TPB_C = C_::TPB_C;
   constexpr int ITEMS = C_::ITEMS;
+  constexpr int RING_O = C_::RING_O;
+  constexpr int RING_N = C_::RING_N;
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   Smem<VT, IPT>& S = *reinterpret_cast<Smem<VT, IPT>*>(smem_raw);
@@ -113,15 +124,14 @@ __global__ void __launch_bounds__(Cfg<IPT>::TPB)
   if (tid == 0) {
     ctl.g = (int)atomicAdd(&hdr->ticket, 1u);
     ctl.epoch = read_epoch(hdr);
-    ctl.abort = 0;
     ctl.pend = 0;
     for (int i = 0; i < K_O; ++i) {
       mbar_init(&S.full_o[i], 1);
-      mbar_init(&S.empty_o[i], 1);
+      mbar_init(&S.empty_o[i], C_::NW_C);
     }
     for (int i = 0; i < K_N; ++i) {
       mbar_init(&S.full_n[i], 1);
-      mbar_init(&S.empty_n[i], 1);
+      mbar_init(&S.empty_n[i], C_::NW_C);
     }
     fence_mbar_init();
   }
@@ -137,52 +147,51 @@ __global__ void __launch_bounds__(Cfg<IPT>::TPB)
     const long long xx = warp_merge_search(a.offsets + 1, a.rows, a.nnz, diag);
     if (lane == 0) {
       if (warp == 0) {
-        ctl.rs = xx;
-        ctl.ns = diag - xx;
+        ctl.rs = (int)xx;
+        ctl.ns = (int)(diag - xx);
       } else {
-        ctl.re = xx;
-        ctl.ne = diag - xx;
+        ctl.re = (int)xx;
+        ctl.ne = (int)(diag - xx);
       }
     }
   }
   __syncthreads();
   if (!active && tid == 0) raise_flag(hdr, EL_FLAG_TIMEOUT, (unsigned)g);
-  const long long rs = ctl.rs, ns = ctl.ns, re = ctl.re, ne = ctl.ne;
-  const long long o_base = rs & ~3LL;  // 16-byte aligned element index
-  const long long n_base = ns & ~7LL;  // 16-byte aligned for 2- and 4-byte
+  const int rs = ctl.rs, ns = ctl.ns, re = ctl.re, ne = ctl.ne;
+  const int o_base = rs & ~3;  // 16-byte aligned element index
+  const int n_base = ns & ~7;  // 16-byte aligned for 2- and 4-byte values
 
   if (warp == C_::WARP_PO) {
     // ------------------------------------------- producer: row offsets
-    const long long o_end = active ? re + 1 : o_base;  // [o_base, re]
-    const long long nch = (o_end - o_base + C - 1) / C;
+    const int o_end = active ? re + 1 : o_base;  // elements [o_base, re]
+    const int nch = (o_end - o_base + C - 1) / C;
     const uint64_t pol = l2_policy_evict_first();
-    long long c = 0;
+    int c = 0;
     bool ok = true;
     for (; c < nch; ++c) {
-      const int slot = (int)(c % K_O);
+      const int slot = c % K_O;
       if (c >= K_O) {
         bool w = true;
         if (lane == 0)
-          w = mbar_wait_bounded(&S.empty_o[slot], (uint32_t)(((c / K_O) - 1) & 1),
-                                a.wait_ns);
+          w = mbar_wait_bounded(&S.empty_o[slot], (uint32_t)(((c / K_O) - 1) & 1), a.wait_ns);
         if (!__shfl_sync(kFullMask, (int)w, 0)) {
           ok = false;
           break;
         }
       }
-      const long long e0 = o_base + c * C;
-      const long long e1 = (e0 + C < o_end) ? e0 + C : o_end;
+      const int e0 = o_base + c * C;
+      const int e1 = min(e0 + C, o_end);
       int* dst = S.ring_o + slot * C;
-      long long eb = e0;  // [e0, eb) by bulk copy, [eb, e1) by plain loads
+      int eb = e0;  // [e0, eb) by bulk copy, [eb, e1) by plain loads
       if (a.tma_o) {
-        const long long up = (e1 + 3) & ~3LL;
-        eb = (up <= a.rows + 1) ? up : (e1 & ~3LL);
+        const int up = (e1 + 3) & ~3;
+        eb = ((long long)up <= a.rows + 1) ? up : (e1 & ~3);
       }
-      for (long long e = eb + lane; e < e1; e += 32) dst[e - e0] = __ldg(a.offsets + e);
+      for (int e = eb + lane; e < e1; e += 32) dst[e - e0] = __ldg(a.offsets + e);
       __syncwarp();
       if (lane == 0) {
         if (eb > e0) {
-          const uint32_t bytes = (uint32_t)((eb - e0) * 4);
+          const uint32_t bytes = (uint32_t)(eb - e0) * 4u;
           mbar_arrive_expect_tx(&S.full_o[slot], bytes);
           bulk_g2s(dst, a.offsets + e0, bytes, &S.full_o[slot], pol);
         } else {
@@ -195,47 +204,46 @@ __global__ void __launch_bounds__(Cfg<IPT>::TPB)
       // no bulk copy may still be landing in shared memory when we leave
       for (int s = 0; s < K_O; ++s)
         if (s < c) {
-          const long long last = s + ((c - 1 - s) / K_O) * K_O;
+          const int last = s + ((c - 1 - s) / K_O) * K_O;
           mbar_wait_bounded(&S.full_o[s], (uint32_t)((last / K_O) & 1), a.wait_ns);
         }
     }
   } else if (warp == C_::WARP_PN) {
     // --------------------------------- producer: (column, value) pairs
-    const long long nch = (active && ne > ns) ? (ne - n_base + C - 1) / C : 0;
+    const int nch = (active && ne > ns) ? (ne - n_base + C - 1) / C : 0;
     const uint64_t pol = l2_policy_evict_first();
     const VT* vals = reinterpret_cast<const VT*>(a.values);
-    long long c = 0;
+    int c = 0;
     bool ok = true;
     for (; c < nch; ++c) {
-      const int slot = (int)(c % K_N);
+      const int slot = c % K_N;
       if (c >= K_N) {
         bool w = true;
         if (lane == 0)
-          w = mbar_wait_bounded(&S.empty_n[slot], (uint32_t)(((c / K_N) - 1) & 1),
-                                a.wait_ns);
+          w = mbar_wait_bounded(&S.empty_n[slot], (uint32_t)(((c / K_N) - 1) & 1), a.wait_ns);
         if (!__shfl_sync(kFullMask, (int)w, 0)) {
           ok = false;
           break;
         }
       }
-      const long long e0 = n_base + c * C;
-      const long long e1 = (e0 + C < ne) ? e0 + C : ne;
+      const int e0 = n_base + c * C;
+      const int e1 = min(e0 + C, ne);
       int* dc = S.ring_c + slot * C;
       VT* dv = S.ring_v + slot * C;
-      long long eb = e0;
+      int eb = e0;
       if (a.tma_n) {
-        const long long up = (e1 + 7) & ~7LL;
-        eb = (up <= a.nnz) ? up : (e1 & ~7LL);
+        const int up = (e1 + 7) & ~7;
+        eb = ((long long)up <= a.nnz) ? up : (e1 & ~7);
       }
-      for (long long e = eb + lane; e < e1; e += 32) {
+      for (int e = eb + lane; e < e1; e += 32) {
         dc[e - e0] = __ldg(a.indices + e);
         dv[e - e0] = vals[e];
       }
       __syncwarp();
       if (lane == 0) {
         if (eb > e0) {
-          const uint32_t bc = (uint32_t)((eb - e0) * 4);
-          const uint32_t bv = (uint32_t)((eb - e0) * sizeof(VT));
+          const uint32_t bc = (uint32_t)(eb - e0) * 4u;
+          const uint32_t bv = (uint32_t)(eb - e0) * (uint32_t)sizeof(VT);
           mbar_arrive_expect_tx(&S.full_n[slot], bc + bv);
           bulk_g2s(dc, a.indices + e0, bc, &S.full_n[slot], pol);
           bulk_g2s(dv, vals + e0, bv, &S.full_n[slot], pol);
@@ -248,104 +256,104 @@ __global__ void __launch_bounds__(Cfg<IPT>::TPB)
       if (!ok) raise_flag(hdr, EL_FLAG_TIMEOUT, 2);
       for (int s = 0; s < K_N; ++s)
         if (s < c) {
-          const long long last = s + ((c - 1 - s) / K_N) * K_N;
+          const int last = s + ((c - 1 - s) / K_N) * K_N;
           mbar_wait_bounded(&S.full_n[s], (uint32_t)((last / K_N) & 1), a.wait_ns);
         }
     }
   } else {
     // ------------------------------------------------------- consumers
-    auto ring_off = [&](long long e) -> int {
-      const long long d = e - o_base;
-      return S.ring_o[(int)((d >> C_::LOG_C) % K_O) * C + (int)(d & (C - 1))];
-    };
-    auto ring_pos_n = [&](long long e) -> int {
-      const long long d = e - n_base;
-      return (int)((d >> C_::LOG_C) % K_N) * C + (int)(d & (C - 1));
-    };
     const float* __restrict__ scale = a.row_scale;
-    long long o_ready = 0, n_ready = 0, o_rel = 0, n_rel = 0;
-    long long r0 = rs, n0 = ns;
-    const long long d_end = active ? re + ne : rs + ns;
+    int o_ready = 0, n_ready = 0, o_rel = 0, n_rel = 0;  // chunk counters
+    int r0 = rs, n0 = ns;
+    int po = rs - o_base;  // ring position of offsets[r0]
+    int pn = ns - n_base;  // ring position of nonzero n0
+    const int d_end = active ? re + ne : rs + ns;
     Acc<COMP> carry;  // partial of row r0 carried in from the previous tile
-    bool first_tile = true;
     bool need_lb = false;  // the range starts inside a row begun earlier
     int off_rs = 0;
-    bool bad_walk = false;
+    bool bad = false;
+    bool first_tile = true;
+    int buf = 0;
 
     while (r0 + n0 < d_end) {
-      const long long D = (d_end - (r0 + n0) < ITEMS) ? d_end - (r0 + n0) : ITEMS;
-      const long long a_need = (re - r0 < D) ? re - r0 : D;
-      const long long b_need = (ne - n0 < D) ? ne - n0 : D;
-      const long long co = (r0 + a_need - o_base) >> C_::LOG_C;
-      const long long cn = b_need > 0 ? (n0 + b_need - 1 - n_base) >> C_::LOG_C : -1;
-      if (tid == 0) {
-        bool ok = true;
-        for (long long c = o_ready; ok && c <= co; ++c)
-          ok = mbar_wait_bounded(&S.full_o[c % K_O], (uint32_t)((c / K_O) & 1), a.wait_ns);
-        for (long long c = n_ready; ok && c <= cn; ++c)
-          ok = mbar_wait_bounded(&S.full_n[c % K_N], (uint32_t)((c / K_N) & 1), a.wait_ns);
-        if (!ok) {
-          ctl.abort = 1;
-          raise_flag(hdr, EL_FLAG_TIMEOUT, 3);
-        }
+      const int D = min(ITEMS, d_end - (r0 + n0));
+      const int a_need = min(D, re - r0);  // row ends that may fall in the tile
+      const int b_need = min(D, ne - n0);
+      // every consumer thread waits for the offsets [r0, r0 + a_need]
+      bool late = false;
+      {
+        const int co = (r0 + a_need - o_base) >> C_::LOG_C;
+        for (; o_ready <= co; ++o_ready)
+          if (!mbar_wait_bounded(&S.full_o[o_ready % K_O], (uint32_t)((o_ready / K_O) & 1),
+                                 a.wait_ns))
+            late = true;
       }
-      named_bar_sync(1, TPB_C);
-      if (ctl.abort) break;
-      if (co + 1 > o_ready) o_ready = co + 1;
-      if (cn + 1 > n_ready) n_ready = cn + 1;
+      // offsets[r0 + 1 + k] from the ring
+      auto row_end = [&](int k) { return S.ring_o[wrap(po + 1 + k, RING_O)]; };
       if (first_tile) {
-        off_rs = ring_off(rs);
+        off_rs = S.ring_o[po];
         need_lb = ns > off_rs;
       }
-
-      // split point of the tile end, then of this thread's first item
-      auto tile_a = [&](long long k) { return ring_off(r0 + 1 + k); };
-      const long long X = seq_merge_search(tile_a, a_need, n0, b_need, D);
-      const long long Y = D - X;
-      const long long diag_t = (long long)tid * IPT;
-      long long tx = X, ty = Y;
-      if (diag_t < D) {
-        const long long f = seq_merge_search(tile_a, X, n0, Y, diag_t);
-        tx = f;
-        ty = diag_t - f;
+      // tile end: X row ends among the next D items.  Row end k sits at merge
+      // position p_k = k + row_end(k) - n0; X = first k with p_k >= D.
+      const int x_min = max(D - b_need, 0);
+      const int X =
+          warp_lower_bound(x_min, a_need, [&](int k) { return k + row_end(k) - n0 < D; });
+      const int Y = D - X;
+      {
+        const int cn = Y > 0 ? (n0 + Y - 1 - n_base) >> C_::LOG_C : -1;
+        for (; n_ready <= cn; ++n_ready)
+          if (!mbar_wait_bounded(&S.full_n[n_ready % K_N], (uint32_t)((n_ready / K_N) & 1),
+                                 a.wait_ns))
+            late = true;
       }
-
-      // products of the tile's nonzeros: one gather of x per nonzero
-      for (long long j = tid; j < Y; j += TPB_C) {
-        const int pos = ring_pos_n(n0 + j);
-        const int col = S.ring_c[pos];
+      // products of the tile's nonzeros: one gather of x each
+      float* prod = S.prod[buf];
+      for (int j = tid; j < Y; j += TPB_C) {
+        const int q = wrap(pn + j, RING_N);
+        const int col = S.ring_c[q];
         float p = 0.f;
         if ((unsigned)col < (unsigned long long)a.cols)
-          p = __fmul_rn(to_f32(S.ring_v[pos]), __ldg(a.x + col));
+          p = __fmul_rn(to_f32(S.ring_v[q]), __ldg(a.x + col));
         else
           raise_flag(hdr, EL_FLAG_INDEX_RANGE, (unsigned)(n0 + j));
-        S.prod[j] = p;
+        prod[j] = p;
       }
-      named_bar_sync(1, TPB_C);
+      // split points: thread t starts at row sx[t] = #{k : p_k < t * IPT}
+      int* sx = S.sx[buf];
+      for (int k = tid; k <= X; k += TPB_C) {
+        int hi = TPB_C - 1, lo = 0;
+        if (k < X) hi = min(max(k + row_end(k) - n0, 0) / IPT, TPB_C - 1);
+        if (k > 0) lo = min(max(k - 1 + row_end(k - 1) - n0, 0) / IPT, TPB_C - 1) + 1;
+        for (int t = lo; t <= hi; ++t) sx[t] = k;
+      }
+      if (tid == 0) sx[TPB_C] = X;
+      if (named_bar_or(2, TPB_C, late)) {  // uniform: every thread sees it
+        if (tid == 0) raise_flag(hdr, EL_FLAG_TIMEOUT, 3);
+        break;
+      }
 
       // walk this thread's IPT merge items
       Acc<COMP> run;
       int first_x = -1;
       Acc<COMP> first_v;
       {
-        long long x = tx, y = ty;
-        const long long steps = D - diag_t;
+        // x <= tid * IPT and xe <= X hold for every valid CSR; the clamps
+        // keep a malformed one inside the tile's arrays
+        int x = min(sx[tid], tid * IPT);
+        const int xe = min(sx[tid + 1], X);
+        int y = tid * IPT - x;
+        const int steps = D - tid * IPT;
 #pragma unroll
         for (int i = 0; i < IPT; ++i) {
           if (i < steps) {
-            bool rowend;
-            if (x >= X)
-              rowend = false;
-            else if (y >= Y)
-              rowend = true;
-            else
-              rowend = (n0 + y) >= (long long)ring_off(r0 + x + 1);
+            const bool rowend = x < xe && (y >= Y || n0 + y >= row_end(x));
             if (rowend) {
               if (first_x < 0) {
-                first_x = (int)x;
+                first_x = x;
                 first_v = run;
               } else {
-                const long long r = r0 + x;
+                const int r = r0 + x;
                 float v = run.value();
                 if (scale) v *= __ldg(scale + r);
                 a.y[r] = v;
@@ -353,10 +361,10 @@ __global__ void __launch_bounds__(Cfg<IPT>::TPB)
               run = Acc<COMP>();
               ++x;
             } else if (y < Y) {
-              run.add(S.prod[y]);
+              run.add(prod[y]);
               ++y;
             } else {
-              bad_walk = true;
+              bad = true;
             }
           }
         }
@@ -380,40 +388,48 @@ __global__ void __launch_bounds__(Cfg<IPT>::TPB)
           ctl.pend_s = v.s;
           ctl.pend_c = v.comp();
         } else {
-          const long long r = r0 + first_x;
+          const int r = r0 + first_x;
           float vv = v.value();
           if (scale) vv *= __ldg(scale + r);
           a.y[r] = vv;
         }
       }
       carry = tot.v;
-      named_bar_sync(1, TPB_C);  // ring, products and scan scratch are free
 
-      const long long r1 = r0 + X, n1 = n0 + Y;
-      const long long orel = (r1 - o_base) >> C_::LOG_C;
-      const long long nrel = (n1 - n_base) >> C_::LOG_C;
-      if (tid == 0) {
-        for (long long c = o_rel; c < orel; ++c) mbar_arrive(&S.empty_o[c % K_O]);
-        for (long long c = n_rel; c < nrel; ++c) mbar_arrive(&S.empty_n[c % K_N]);
+      // hand fully consumed chunks back to the producers (one arrival per
+      // warp: a chunk is refilled once all consumer warps are done with it)
+      const int r1 = r0 + X, n1 = n0 + Y;
+      const int orel = (r1 - o_base) >> C_::LOG_C;
+      const int nrel = (n1 - n_base) >> C_::LOG_C;
+      __syncwarp();
+      if (lane == 0) {
+        for (int c = o_rel; c < orel; ++c) mbar_arrive(&S.empty_o[c % K_O]);
+        for (int c = n_rel; c < nrel; ++c) mbar_arrive(&S.empty_n[c % K_N]);
       }
-      if (orel > o_rel) o_rel = orel;
-      if (nrel > n_rel) n_rel = nrel;
+      o_rel = max(o_rel, orel);
+      n_rel = max(n_rel, nrel);
+      po = wrap(po + X, RING_O);
+      pn = wrap(pn + Y, RING_N);
       r0 = r1;
       n0 = n1;
+      buf ^= 1;
       first_tile = false;
     }
-    if (bad_walk) raise_flag(hdr, EL_FLAG_OFFSETS, (unsigned)r0);
+    if (bad) raise_flag(hdr, EL_FLAG_OFFSETS, (unsigned)r0);
+    // every consumer has left the tile loop (and written ctl.pend) before
+    // the end-of-range work reads it
+    named_bar_sync(1, TPB_C);
 
-    if (active && !ctl.abort) {
+    if (active && r0 + n0 >= d_end) {
       if (tid == 0) {
-        const int off_re = ring_off(re);
+        const int off_re = S.ring_o[po];  // offsets[re]
         if (g == 0 && off_rs != 0) raise_flag(hdr, EL_FLAG_NNZ_MISMATCH, 0);
-        if (re == a.rows && off_re != a.nnz)
+        if ((long long)re == a.rows && (long long)off_re != a.nnz)
           raise_flag(hdr, EL_FLAG_NNZ_MISMATCH, (unsigned)re);
         // publish the partial of the row still open at the range end, if
         // this range holds any of its nonzeros; exactly one later range
-        // (the one where the row ends) reads and clears it
-        const long long lo = (long long)off_re > ns ? (long long)off_re : ns;
+        // (the one where the row ends) reads it
+        const int lo = max(off_re, ns);
         if (ne > lo && g < a.ws.nslots && !(a.test_hooks & 1)) {
           CarrySlot* sl = a.ws.slots + g;
           sl->sum = carry.s;
@@ -425,7 +441,7 @@ __global__ void __launch_bounds__(Cfg<IPT>::TPB)
         // the row rs began in range gfirst: sum the partials of ranges
         // [gfirst, g) in a fixed order (each published with this launch's
         // tag; exactly this range reads them)
-        const long long gfirst = (rs + off_rs) / a.range_items;
+        const long long gfirst = ((long long)rs + off_rs) / a.range_items;
         Acc<COMP> acc;
         bool ok = true;
         for (long long k = gfirst + lane; k < g && k < a.ws.nslots; k += 32) {
@@ -471,7 +487,7 @@ __global__ void __launch_bounds__(Cfg<IPT>::TPB)
     }
   }
 
-  // the last CTA to finish hands the workspace back in its initial state
+  // the last CTA to finish hands the workspace back for the next launch
   __syncthreads();
   if (tid == 0) {
     __threadfence();

@@ -199,11 +199,69 @@ el_status el_work_oriented_partition(const int32_t* offsets, int64_t rows,
                                      int64_t nnz, int64_t num_threads,
                                      int64_t* coords, el_stream_t stream);
 
+/* ---- batched SpMV (no counterpart in the reference) --------------------
+ * Thousands of independent CSR matrices, each with its own x and y, run in
+ * ONE persistent launch that the plan captures in a CUDA graph.  A plan
+ * computes row-length statistics of every matrix on the device, picks per
+ * matrix a threads-per-row and a chunk size from a tuning table indexed by
+ * (rows, mean row length, row-length variation) buckets, splits every
+ * matrix into row chunks of about that many nonzeros and stores the work
+ * list on the device.  Matrices with a row longer than
+ * EL_BATCH_MAX_ROW_NNZ run as their own merge-path launches inside the same
+ * graph.  All matrices of a plan share one value dtype. */
+typedef struct el_batch_item {
+  el_csr A;
+  const float* x;
+  float* y;
+} el_batch_item;
+
+#define EL_BATCH_ROW_BUCKETS 21 /* floor(log2(rows)), clamped to [0, 20] */
+#define EL_BATCH_LEN_BUCKETS 11 /* mean nnz/row: < 1, [1,2), [2,4), ... , >= 512 */
+#define EL_BATCH_CV_BUCKETS 4   /* row-length std/mean: < .25, < .75, < 1.5, >= 1.5 */
+#define EL_BATCH_TABLE_SIZE \
+  (EL_BATCH_ROW_BUCKETS * EL_BATCH_LEN_BUCKETS * EL_BATCH_CV_BUCKETS)
+/* table index = (row_bucket * EL_BATCH_LEN_BUCKETS + len_bucket) *
+ * EL_BATCH_CV_BUCKETS + cv_bucket; entry = threads_per_row (1..32) |
+ * log2(nonzeros per work item) << 8, or 0 for the built-in rule. */
+#define EL_BATCH_MAX_ROW_NNZ 16384
+
+typedef struct el_batch_opts {
+  const int32_t* table;          /* EL_BATCH_TABLE_SIZE entries or NULL */
+  int32_t use_graph;             /* 1: capture in a CUDA graph (default 1 via
+                                    el_batch_opts_default) */
+  int32_t force_threads_per_row; /* > 0: this for every matrix (tuning) */
+  int32_t force_chunk_log2;      /* > 0: this for every matrix (tuning) */
+  int32_t max_ctas;              /* cap on the persistent grid (0 = resident) */
+  int32_t reserved[8];
+} el_batch_opts;
+
+typedef struct el_batch_plan el_batch_plan;
+
+void el_batch_opts_default(el_batch_opts* opts);
+/* items: host array of `count` matrices.  Synchronises `stream` (it reads
+ * the statistics back); the inputs must stay valid while the plan lives. */
+el_status el_batch_plan_create(const el_batch_item* items, int32_t count,
+                               const el_batch_opts* opts, el_stream_t stream,
+                               el_batch_plan** out);
+/* One y = A x for every matrix of the plan, asynchronous on `stream`. */
+el_status el_batch_plan_execute(el_batch_plan* plan, el_stream_t stream);
+/* Work items, matrices per threads-per-row value (tpr_counts[6] for
+ * 1,2,4,8,16,32) and matrices run as separate merge-path launches. */
+el_status el_batch_plan_info(const el_batch_plan* plan, int64_t* work_items,
+                             int32_t* tpr_counts, int32_t* heavy);
+/* Synchronises `stream` and returns (and optionally clears) the EL_FLAG_*
+ * bits raised by the plan's kernels. */
+el_status el_batch_plan_errors(el_batch_plan* plan, el_stream_t stream,
+                               uint32_t* flags, int clear);
+el_status el_batch_plan_destroy(el_batch_plan* plan);
+
 /* ---- mixed precision -------------------------------------------------- */
 /* Converts FP32 values to BF16 / FP16 (round to nearest even).  With
  * row_scale != NULL, each row is first divided by a power of two chosen so
- * that the row's largest magnitude lands in [1, 2) and the power is written
- * to row_scale[row] (exact: dequantised = out * row_scale). */
+ * that the row's largest magnitude lands in [1, 2) for BF16 or in
+ * [2^14, 2^15) for FP16 (the top of its range, so the row's small entries
+ * stay clear of FP16 subnormals), and the power is written to
+ * row_scale[row] (exact: dequantised = out * row_scale). */
 el_status el_quantize_values(const int32_t* offsets, int64_t rows,
                              int64_t nnz, const float* values, int32_t dtype,
                              void* out_values, float* row_scale,
