@@ -61,7 +61,8 @@ class ElSpmvOpts(C.Structure):
         ("max_ctas", C.c_int32),
         ("wait_limit_us", C.c_int32),
         ("test_hooks", C.c_int32),
-        ("reserved", C.c_int32 * 6),
+        ("variant", C.c_int32),
+        ("reserved", C.c_int32 * 5),
     ]
 
 

@@ -134,7 +134,11 @@ typedef struct el_spmv_opts {
                                 merge_path ranges skip publishing their row
                                 carries, so a range that needs one waits until
                                 wait_limit_us and reports EL_FLAG_TIMEOUT */
-  int32_t reserved[6];
+  int32_t variant;           /* merge_path kernel: 0 = warp-streaming (each
+                                warp walks its own range, register prefetch);
+                                1 = CTA ring (producer warps stream the
+                                range into shared memory with bulk copies) */
+  int32_t reserved[5];
 } el_spmv_opts;
 
 typedef struct el_workspace el_workspace;

@@ -15,8 +15,10 @@ pytestmark = pytest.mark.gpu
 
 SCHEDS = [
     ("merge_path_flat", {}),
-    ("merge_path_flat", {"items_per_thread": 4}),
     ("merge_path_flat", {"compensated": True}),
+    ("merge_path_flat", {"variant": 1}),
+    ("merge_path_flat", {"variant": 1, "items_per_thread": 4}),
+    ("merge_path_flat", {"variant": 1, "compensated": True}),
     ("work_oriented", {}),
     ("thread_mapped", {}),
     ("thread_mapped", {"threads_per_row": 8}),
@@ -123,8 +125,10 @@ def test_long_rows_across_many_ctas(cuda, oracle_mod):
     off, idx, vals, x = random_csr(rng, rows=400, cols=300_000, max_len=50,
                                    long_rows=[(0, 250_000), (17, 120_000), (399, 200_000)])
     A = dev_csr(off, idx, vals, 300_000, cuda)
-    for opts in ({"items_per_thread": 4}, {"items_per_thread": 4, "max_ctas": 7},
-                 {"max_ctas": 1}, {"compensated": True}):
+    for opts in ({}, {"max_ctas": 3}, {"max_ctas": 1}, {"compensated": True},
+                 {"variant": 1, "items_per_thread": 4},
+                 {"variant": 1, "items_per_thread": 4, "max_ctas": 7},
+                 {"variant": 1, "max_ctas": 1}, {"variant": 1, "compensated": True}):
         y, flags = run(A, x, "merge_path_flat", opts, cuda)
         assert flags == 0
         check_against_oracle(oracle_mod, off, idx, vals, x, y)
