@@ -174,6 +174,8 @@ def run_ours(args, rank, world):
                                      row_scale=A.row_scale is not None)
     ws = api.Workspace()
     opts = dict(items_per_thread=args.ipt) if args.ipt else {}
+    if args.variant:
+        opts["variant"] = args.variant
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
 
@@ -440,6 +442,8 @@ def main():
     ap.add_argument("--schedule", default="merge_path_flat")
     ap.add_argument("--value-dtype", default="f32", choices=["f32", "bf16", "f16"])
     ap.add_argument("--ipt", type=int, default=0)
+    ap.add_argument("--variant", type=int, default=0,
+                    help="merge_path kernel: 0 warp-streaming, 1 CTA ring")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     args = ap.parse_args()

@@ -330,6 +330,39 @@ __device__ __forceinline__ SegVal<COMP> seg_combine(const SegVal<COMP>& a,
   return r;
 }
 
+// Warp shuffles of an accumulator (the compensation term only when there
+// is one).
+__device__ __forceinline__ Acc<false> shfl_up_acc(const Acc<false>& a, int d) {
+  Acc<false> r;
+  r.s = __shfl_up_sync(kFullMask, a.s, d);
+  return r;
+}
+__device__ __forceinline__ Acc<true> shfl_up_acc(const Acc<true>& a, int d) {
+  Acc<true> r;
+  r.set(__shfl_up_sync(kFullMask, a.s, d), __shfl_up_sync(kFullMask, a.c, d));
+  return r;
+}
+__device__ __forceinline__ Acc<false> shfl_idx_acc(const Acc<false>& a, int src) {
+  Acc<false> r;
+  r.s = __shfl_sync(kFullMask, a.s, src);
+  return r;
+}
+__device__ __forceinline__ Acc<true> shfl_idx_acc(const Acc<true>& a, int src) {
+  Acc<true> r;
+  r.set(__shfl_sync(kFullMask, a.s, src), __shfl_sync(kFullMask, a.c, src));
+  return r;
+}
+__device__ __forceinline__ Acc<false> shfl_xor_acc(const Acc<false>& a, int m) {
+  Acc<false> r;
+  r.s = __shfl_xor_sync(kFullMask, a.s, m);
+  return r;
+}
+__device__ __forceinline__ Acc<true> shfl_xor_acc(const Acc<true>& a, int m) {
+  Acc<true> r;
+  r.set(__shfl_xor_sync(kFullMask, a.s, m), __shfl_xor_sync(kFullMask, a.c, m));
+  return r;
+}
+
 // Inclusive warp-level segmented scan.
 template <bool COMP>
 __device__ __forceinline__ SegVal<COMP> warp_seg_scan(SegVal<COMP> me) {
@@ -338,8 +371,7 @@ __device__ __forceinline__ SegVal<COMP> warp_seg_scan(SegVal<COMP> me) {
   for (int d = 1; d < 32; d <<= 1) {
     SegVal<COMP> o;
     o.f = __shfl_up_sync(kFullMask, me.f, d);
-    o.v.set(__shfl_up_sync(kFullMask, me.v.s, d),
-            __shfl_up_sync(kFullMask, me.v.comp(), d));
+    o.v = shfl_up_acc(me.v, d);
     if (lane >= d) me = seg_combine(o, me);
   }
   return me;
@@ -384,8 +416,7 @@ __device__ __forceinline__ SegVal<COMP> block_seg_scan_excl(
   // exclusive within the warp: the inclusive value of lane-1
   SegVal<COMP> ex;
   ex.f = __shfl_up_sync(kFullMask, inc.f, 1);
-  ex.v.set(__shfl_up_sync(kFullMask, inc.v.s, 1),
-           __shfl_up_sync(kFullMask, inc.v.comp(), 1));
+  ex.v = shfl_up_acc(inc.v, 1);
   SegVal<COMP> out = (lane == 0) ? pre : seg_combine(pre, ex);
   *total = tot;
   return out;

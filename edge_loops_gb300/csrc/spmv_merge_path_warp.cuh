@@ -30,9 +30,7 @@
 namespace el {
 namespace mpw {
 
-constexpr int kIPT = 8;
-constexpr int kTile = 32 * kIPT;  // merge items per warp tile
-constexpr int kWarps = 8;         // warps per CTA
+constexpr int kWarps = 8;  // warps per CTA
 constexpr int kTPB = 32 * kWarps;
 
 struct Args {
@@ -43,13 +41,14 @@ struct Args {
   const float* row_scale;
   const float* x;
   float* y;
-  long long range_items;  // merge items per warp range (multiple of kTile)
+  long long range_items;  // merge items per warp range (multiple of the tile)
   long long num_ranges;
   unsigned long long wait_ns;
   int test_hooks;
   WsView ws;
 };
 
+template <int kTile>
 struct WarpSmem {
   float prod[kTile];     // products of the tile's nonzeros
   int re[kTile + 1];     // tile-local row ends: offsets[r0+1+k] - n0
@@ -75,12 +74,15 @@ __device__ __forceinline__ __half ld_stream<__half>(const __half* p) {
   return __ushort_as_half(u);
 }
 
-template <typename VT, bool COMP>
-__global__ void __launch_bounds__(kTPB)
+// IPT merge items per lane (tile = 32 * IPT); MINB resident CTAs per SM
+// the register allocation must allow.
+template <typename VT, int kIPT, bool COMP, int MINB>
+__global__ void __launch_bounds__(kTPB, MINB)
     merge_path_warp_kernel(const Args a) {
-  __shared__ WarpSmem smem_all[kWarps];
+  constexpr int kTile = 32 * kIPT;
+  __shared__ WarpSmem<kTile> smem_all[kWarps];
   const int lane = threadIdx.x & 31;
-  WarpSmem& S = smem_all[threadIdx.x >> 5];
+  WarpSmem<kTile>& S = smem_all[threadIdx.x >> 5];
   WsHeader* hdr = a.ws.hdr;
   const VT* vals = reinterpret_cast<const VT*>(a.values);
   const float* __restrict__ scale = a.row_scale;
@@ -118,15 +120,25 @@ __global__ void __launch_bounds__(kTPB)
     auto load_window = [&](int r, int n, int& o, int (&cc)[kIPT], VT (&vv)[kIPT]) {
       const int k = r + 1 + lane;
       o = k <= rows ? __ldcs(a.offsets + k) : 0x7fffffff;
+      if (n + kTile <= nnz) {  // whole window inside the arrays
+        const int* ip = a.indices + n + lane;
+        const VT* vp = vals + n + lane;
 #pragma unroll
-      for (int i = 0; i < kIPT; ++i) {
-        const int e = n + lane + 32 * i;
-        if (e < nnz) {
-          cc[i] = __ldcs(a.indices + e);
-          vv[i] = ld_stream<VT>(vals + e);
-        } else {
-          cc[i] = -1;
-          vv[i] = VT(0.f);
+        for (int i = 0; i < kIPT; ++i) {
+          cc[i] = __ldcs(ip + 32 * i);
+          vv[i] = ld_stream<VT>(vp + 32 * i);
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < kIPT; ++i) {
+          const int e = n + lane + 32 * i;
+          if (e < nnz) {
+            cc[i] = __ldcs(a.indices + e);
+            vv[i] = ld_stream<VT>(vals + e);
+          } else {
+            cc[i] = -1;
+            vv[i] = VT(0.f);
+          }
         }
       }
     };
@@ -160,10 +172,6 @@ __global__ void __launch_bounds__(kTPB)
       }
       const int Y = D - X;
 
-      // start loading the next tile while this one computes
-      int n_o = 0, n_c[kIPT];
-      VT n_v[kIPT];
-      if (r0 + n0 + D < d1) load_window(r0 + X, n0 + Y, n_o, n_c, n_v);
 
       // products of the tile's nonzeros (nonzero j of the tile is register
       // i = j / 32 of lane j % 32)
@@ -180,6 +188,9 @@ __global__ void __launch_bounds__(kTPB)
           S.prod[j] = p;
         }
       }
+      // the window registers are consumed: load the next tile's window into
+      // them now, so the loads overlap this tile's split, walk and scan
+      if (r0 + n0 + D < d1) load_window(r0 + X, n0 + Y, o_reg, c_reg, v_reg);
       __syncwarp();  // the row ends in S.re come from every lane
       // split points: lane t starts at row sx[t] = #{k : p_k < t * kIPT}
       for (int k = lane; k <= X; k += 32) {
@@ -199,11 +210,13 @@ __global__ void __launch_bounds__(kTPB)
         const int xe = min(S.sx[lane + 1], X);
         int y = lane * kIPT - x;
         const int steps = D - lane * kIPT;
+        // tile-local nonzero position where the lane's current row ends
+        // (past the end: the lane has no row end left)
+        int nre = x < xe ? min(S.re[x], Y) : 0x7fffffff;
 #pragma unroll
         for (int i = 0; i < kIPT; ++i) {
           if (i < steps) {
-            const bool rowend = x < xe && (y >= Y || y >= S.re[x]);
-            if (rowend) {
+            if (y >= nre) {
               if (first_x < 0) {
                 first_x = x;
                 first_v = run;
@@ -215,6 +228,7 @@ __global__ void __launch_bounds__(kTPB)
               }
               run = Acc<COMP>();
               ++x;
+              nre = x < xe ? min(S.re[x], Y) : 0x7fffffff;
             } else if (y < Y) {
               run.add(S.prod[y]);
               ++y;
@@ -232,7 +246,7 @@ __global__ void __launch_bounds__(kTPB)
       const SegVal<COMP> inc = warp_seg_scan<COMP>(mine);
       SegVal<COMP> ex;
       ex.f = __shfl_up_sync(kFullMask, inc.f, 1);
-      ex.v.set(__shfl_up_sync(kFullMask, inc.v.s, 1), __shfl_up_sync(kFullMask, inc.v.comp(), 1));
+      ex.v = shfl_up_acc(inc.v, 1);
       SegVal<COMP> cin;
       cin.f = 0;
       cin.v = carry;
@@ -254,16 +268,10 @@ __global__ void __launch_bounds__(kTPB)
         }
       }
       const SegVal<COMP> all = seg_combine(cin, inc);  // carry (+) lanes 0..lane
-      carry.set(__shfl_sync(kFullMask, all.v.s, 31), __shfl_sync(kFullMask, all.v.comp(), 31));
+      carry = shfl_idx_acc(all.v, 31);
 
       r0 += X;
       n0 += Y;
-      o_reg = n_o;
-#pragma unroll
-      for (int i = 0; i < kIPT; ++i) {
-        c_reg[i] = n_c[i];
-        v_reg[i] = n_v[i];
-      }
       __syncwarp();  // shared scratch is reused by the next tile
     }
     if (__any_sync(kFullMask, bad) && lane == 0) raise_flag(hdr, EL_FLAG_OFFSETS, (unsigned)r0);
@@ -306,8 +314,7 @@ __global__ void __launch_bounds__(kTPB)
       }
 #pragma unroll
       for (int d = 16; d > 0; d >>= 1) {
-        Acc<COMP> o;
-        o.set(__shfl_xor_sync(kFullMask, acc.s, d), __shfl_xor_sync(kFullMask, acc.comp(), d));
+        Acc<COMP> o = shfl_xor_acc(acc, d);
         if ((lane & d) == 0) {
           acc.add(o);
         } else {
@@ -337,18 +344,19 @@ __global__ void __launch_bounds__(kTPB)
   }
 }
 
-template <typename VT, bool COMP>
+template <typename VT, int kIPT, bool COMP, int MINB>
 int resident_warps(int device) {
-  const int per_sm =
-      resident_ctas_per_sm((const void*)merge_path_warp_kernel<VT, COMP>, kTPB, 0);
+  const int per_sm = resident_ctas_per_sm(
+      (const void*)merge_path_warp_kernel<VT, kIPT, COMP, MINB>, kTPB, 0);
   return (per_sm > 0 ? per_sm : 1) * kWarps * device_info(device).sm_count;
 }
 
-template <typename VT, bool COMP>
+template <typename VT, int kIPT, bool COMP, int MINB>
 el_status launch(const SpmvCall& c) {
+  constexpr int kTile = 32 * kIPT;
   const long long total = c.A.rows + c.A.nnz;
   const long long tiles = (total + kTile - 1) / kTile;
-  long long W = resident_warps<VT, COMP>(c.device);
+  long long W = resident_warps<VT, kIPT, COMP, MINB>(c.device);
   if (c.o.max_ctas > 0 && (long long)c.o.max_ctas * kWarps < W) W = (long long)c.o.max_ctas * kWarps;
   if (W > tiles) W = tiles;
   if (W < 1) W = 1;
@@ -371,13 +379,13 @@ el_status launch(const SpmvCall& c) {
   if (a.num_ranges > c.ws.nslots)
     return fail(EL_ERR_INVALID_ARGUMENT, "merge_path: workspace too small");
   const long long grid = (a.num_ranges + kWarps - 1) / kWarps;
-  merge_path_warp_kernel<VT, COMP><<<(unsigned)grid, kTPB, 0, c.stream>>>(a);
+  merge_path_warp_kernel<VT, kIPT, COMP, MINB><<<(unsigned)grid, kTPB, 0, c.stream>>>(a);
   return cuda_status(cudaGetLastError(), "merge_path launch");
 }
 
-template <typename VT, bool COMP>
+template <typename VT, int kIPT, bool COMP, int MINB>
 long long slots_needed(const SpmvCall& c) {
-  return resident_warps<VT, COMP>(c.device);
+  return resident_warps<VT, kIPT, COMP, MINB>(c.device);
 }
 
 }  // namespace mpw
