@@ -4,6 +4,7 @@
 #pragma once
 
 #include "spmv_merge_path.cuh"
+#include "spmv_merge_path_nz.cuh"
 #include "spmv_merge_path_warp.cuh"
 #include "spmv_schedules.cuh"
 
@@ -14,13 +15,15 @@ struct SpmvImpl {
   static el_status merge_path(const SpmvCall& c) {
     const int ipt = c.o.items_per_thread;
     const bool comp = c.o.compensated != 0;
-    if (c.o.variant == 0) {
+    if (c.o.variant == 0)
+      return comp ? mpn::launch<VT, true>(c) : mpn::launch<VT, false>(c);
+    if (c.o.variant == 2) {
       if (ipt >= 12)
         return comp ? mpw::launch<VT, 16, true, 2>(c) : mpw::launch<VT, 16, false, 3>(c);
       return comp ? mpw::launch<VT, 8, true, 4>(c) : mpw::launch<VT, 8, false, 5>(c);
     }
     if (c.o.variant != 1)
-      return fail(EL_ERR_INVALID_ARGUMENT, "merge_path variant must be 0 or 1");
+      return fail(EL_ERR_INVALID_ARGUMENT, "merge_path variant must be 0, 1 or 2");
     if (ipt > 0 && ipt <= 4)
       return comp ? mp::launch<VT, 4, true>(c) : mp::launch<VT, 4, false>(c);
     return comp ? mp::launch<VT, 8, true>(c) : mp::launch<VT, 8, false>(c);
@@ -28,7 +31,9 @@ struct SpmvImpl {
   static long long merge_path_slots(const SpmvCall& c) {
     const int ipt = c.o.items_per_thread;
     const bool comp = c.o.compensated != 0;
-    if (c.o.variant == 0) {
+    if (c.o.variant == 0)
+      return comp ? mpn::slots_needed<VT, true>(c) : mpn::slots_needed<VT, false>(c);
+    if (c.o.variant == 2) {
       if (ipt >= 12)
         return comp ? mpw::slots_needed<VT, 16, true, 2>(c)
                     : mpw::slots_needed<VT, 16, false, 3>(c);

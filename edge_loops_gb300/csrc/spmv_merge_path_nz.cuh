@@ -1,0 +1,407 @@
+// spmv_merge_path_nz.cuh -- merge-path SpMV for sm_103a, nonzero-tiled warp
+// variant (the default).
+//
+// The work split follows the reference's merge_path_flat schedule at the
+// level of warp ranges [include/loops/schedule/merge_path_flat.hxx:108-138,
+// util/search.hxx:34-60]: the merge of row ends and nonzeros is cut at
+// global diagonals g * range_items, every warp taking one range (id from an
+// atomic ticket, so a range only ever waits on ranges already running), so
+// every warp gets the same number of rows + nonzeros.  Inside its range a
+// warp walks TILES OF 256 NONZEROS (aligned to multiples of 256), lane l
+// owning the 8 consecutive nonzeros 8l..8l+7 of the tile:
+//
+//   * a lane loads its 8 column indices and 8 values with 128-bit vector
+//     loads straight into registers (the next tile's loads are issued while
+//     the current tile reduces), gathers x and forms 8 products;
+//   * the rows that end inside the tile come from a window of row offsets
+//     (one ballot per 32 rows) as a sorted list of end positions in shared
+//     memory; a lane adds its products in order and closes a row whenever
+//     an end position is reached (empty rows: several ends at one position);
+//   * rows crossing lanes are stitched by a warp segmented scan, rows
+//     crossing tiles by a register carry, rows crossing ranges by carries
+//     that the range where the row ends collects (bounded spins, fixed
+//     order: deterministic).  No CTA barrier anywhere.  y is overwritten.
+#pragma once
+
+#include "el_internal.h"
+
+namespace el {
+namespace mpn {
+
+constexpr int kPer = 8;               // nonzeros per lane
+constexpr int kTileNz = 32 * kPer;    // nonzeros per tile
+constexpr int kMaxEnds = 256;         // row ends per tile (tiles are cut short
+                                      // after this many, e.g. empty rows)
+constexpr int kWarps = 8;
+constexpr int kTPB = 32 * kWarps;
+
+struct Args {
+  long long rows, cols, nnz;
+  const int* offsets;
+  const int* indices;
+  const void* values;
+  const float* row_scale;
+  const float* x;
+  float* y;
+  long long range_items;  // merge items per warp range
+  long long num_ranges;
+  int vec_ok;             // indices and values 16-byte aligned
+  int test_hooks;
+  unsigned long long wait_ns;
+  WsView ws;
+};
+
+struct WarpSmem {
+  int re[kMaxEnds];  // end position (tile-local nonzero index) of each row end
+  int pend;
+  float pend_s, pend_c;
+};
+
+// 8 consecutive values (16-byte aligned for float: two 128-bit loads; one
+// for 16-bit types), converted to float.
+__device__ __forceinline__ void load8(const float* p, float (&v)[kPer]) {
+  const float4 a = __ldcs(reinterpret_cast<const float4*>(p));
+  const float4 b = __ldcs(reinterpret_cast<const float4*>(p) + 1);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void load8(const __nv_bfloat16* p, float (&v)[kPer]) {
+  const uint4 u = __ldcs(reinterpret_cast<const uint4*>(p));
+  const unsigned w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    v[2 * i] = __uint_as_float(w[i] << 16);
+    v[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
+  }
+}
+__device__ __forceinline__ void load8(const __half* p, float (&v)[kPer]) {
+  const uint4 u = __ldcs(reinterpret_cast<const uint4*>(p));
+  const unsigned w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const __half2 h = *reinterpret_cast<const __half2*>(&w[i]);
+    v[2 * i] = __low2float(h);
+    v[2 * i + 1] = __high2float(h);
+  }
+}
+__device__ __forceinline__ void load8i(const int* p, int (&c)[kPer]) {
+  const int4 a = __ldcs(reinterpret_cast<const int4*>(p));
+  const int4 b = __ldcs(reinterpret_cast<const int4*>(p) + 1);
+  c[0] = a.x; c[1] = a.y; c[2] = a.z; c[3] = a.w;
+  c[4] = b.x; c[5] = b.y; c[6] = b.z; c[7] = b.w;
+}
+
+template <typename VT>
+__device__ __forceinline__ float ld_val(const VT* p) {
+  return to_f32(*p);
+}
+
+template <typename VT, bool COMP>
+__global__ void __launch_bounds__(kTPB, 4)
+    merge_path_nz_kernel(const Args a) {
+  __shared__ WarpSmem smem_all[kWarps];
+  const int lane = threadIdx.x & 31;
+  WarpSmem& S = smem_all[threadIdx.x >> 5];
+  WsHeader* hdr = a.ws.hdr;
+  const VT* vals = reinterpret_cast<const VT*>(a.values);
+  const float* __restrict__ scale = a.row_scale;
+  const int rows = (int)a.rows;
+  const unsigned cols = (unsigned)a.cols;
+
+  unsigned tk = 0, ep = 0;
+  if (lane == 0) {
+    tk = atomicAdd(&hdr->ticket, 1u);
+    ep = read_epoch(hdr);
+  }
+  const long long g = __shfl_sync(kFullMask, tk, 0);
+  const unsigned epoch = __shfl_sync(kFullMask, ep, 0);
+  const unsigned tag = epoch_tag(epoch);
+  const long long total = a.rows + a.nnz;
+
+  if (g < a.num_ranges) {
+    const long long dd0 = g * a.range_items;
+    const int d0 = (int)(dd0 < total ? dd0 : total);
+    const int d1 = (int)(dd0 + a.range_items < total ? dd0 + a.range_items : total);
+    const int rs = (int)warp_merge_search(a.offsets + 1, a.rows, a.nnz, d0);
+    const int ns = d0 - rs;
+    const int re = (int)warp_merge_search(a.offsets + 1, a.rows, a.nnz, d1);
+    const int ne = d1 - re;
+    const int off_rs = __ldg(a.offsets + rs);
+    const bool need_lb = ns > off_rs;
+    if (lane == 0) {
+      S.pend = 0;
+      if (g == 0 && off_rs != 0) raise_flag(hdr, EL_FLAG_NNZ_MISMATCH, 0);
+    }
+
+    // tile [lo, hi): nonzeros up to the next multiple of kTileNz (or ne)
+    auto tile_hi = [&](int l) { return l < ne ? min(ne, (l & ~(kTileNz - 1)) + kTileNz) : l; };
+    int c[kPer];
+    float v[kPer];
+    auto load_tile = [&](int l, int h) {
+      const int j0 = l + kPer * lane;
+      if (a.vec_ok && h - l == kTileNz && (l & 7) == 0) {
+        load8i(a.indices + j0, c);
+        load8(vals + j0, v);
+      } else {
+#pragma unroll
+        for (int i = 0; i < kPer; ++i) {
+          const int j = j0 + i;
+          if (j < h) {
+            c[i] = __ldcs(a.indices + j);
+            v[i] = ld_val(vals + j);
+          } else {
+            c[i] = -1;
+            v[i] = 0.f;
+          }
+        }
+      }
+    };
+    auto load_ends = [&](int r) {  // offsets[r + 1 + lane]: end of row r + lane
+      const int k = r + 1 + lane;
+      return k <= rows ? __ldcs(a.offsets + k) : 0x7fffffff;
+    };
+
+    int ra = rs, lo = ns;  // first row not yet closed; first nonzero of the tile
+    int hi = tile_hi(lo);
+    load_tile(lo, hi);
+    int o = load_ends(ra);
+    Acc<COMP> carry;
+    bool bad = false;
+
+    while (lo < ne || ra < re) {
+      // rows [ra, re) ending at or before hi, at most kMaxEnds of them
+      int X = 0;
+      {
+        int e = o;
+        for (int base = 0;;) {
+          const bool in = ra + base + lane < re && e <= hi;
+          const unsigned b = __ballot_sync(kFullMask, in);
+          const int cnt = b == kFullMask ? 32 : __ffs(~b) - 1;
+          if (lane < cnt) S.re[base + lane] = min(max(e - lo, 0), hi - lo);
+          X = base + cnt;
+          if (cnt < 32 || X >= kMaxEnds) break;
+          base += 32;
+          const int k = ra + base + 1 + lane;
+          e = k <= rows ? __ldg(a.offsets + k) : 0x7fffffff;
+        }
+      }
+      __syncwarp();
+      if (X >= kMaxEnds) hi = lo + S.re[kMaxEnds - 1];  // cut the tile at its 256th row end
+      const int Y = hi - lo;
+      if (X == 0 && Y == 0) {  // no progress possible: malformed offsets
+        bad = true;
+        break;
+      }
+
+      // products of this lane's nonzeros 8 lane + i
+      float p[kPer];
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
+        p[i] = 0.f;
+        if (kPer * lane + i < Y) {
+          const int col = c[i];
+          if ((unsigned)col < cols)
+            p[i] = __fmul_rn(v[i], __ldg(a.x + col));
+          else
+            raise_flag(hdr, EL_FLAG_INDEX_RANGE, (unsigned)(lo + kPer * lane + i));
+        }
+      }
+      // the window registers are free: start loading the next tile
+      const int lo2 = hi, hi2 = tile_hi(hi), ra2 = ra + X;
+      if (lo2 < ne) load_tile(lo2, hi2);
+      if (ra2 < re) o = load_ends(ra2);
+
+      // this lane's row ends: end positions in (8 lane, 8 lane + 8] (lane 0:
+      // also position 0, rows closed before any nonzero of the tile)
+      int k = 0;
+      if (lane > 0) {
+        int lo_ = 0, hi_ = X;
+        while (lo_ < hi_) {
+          const int mid = (lo_ + hi_) >> 1;
+          if (S.re[mid] <= kPer * lane) lo_ = mid + 1; else hi_ = mid;
+        }
+        k = lo_;
+      }
+      int kend = __shfl_down_sync(kFullMask, k, 1);
+      if (lane == 31) kend = X;
+
+      Acc<COMP> run, first_v;
+      int first_k = -1;
+      int nxt = k < kend ? S.re[k] - kPer * lane : 0x7fffffff;
+      auto close_row = [&]() {
+        if (first_k < 0) {
+          first_k = k;
+          first_v = run;
+        } else {
+          const int r = ra + k;
+          float val = run.value();
+          if (scale) val *= __ldg(scale + r);
+          a.y[r] = val;
+        }
+        run = Acc<COMP>();
+        ++k;
+        nxt = k < kend ? S.re[k] - kPer * lane : 0x7fffffff;
+      };
+      while (nxt <= 0) close_row();
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
+        run.add(p[i]);
+        while (nxt == i + 1) close_row();
+      }
+      if (k < kend) {  // ends beyond the lane's nonzeros: malformed offsets
+        bad = true;
+        while (k < kend) close_row();
+      }
+
+      // stitch rows across lanes; lane 0 continues the previous tile's row
+      SegVal<COMP> mine, cin;
+      mine.f = first_k >= 0;
+      mine.v = run;
+      cin.f = 0;
+      cin.v = carry;
+      const SegVal<COMP> inc = warp_seg_scan<COMP>(mine);
+      SegVal<COMP> ex;
+      ex.f = __shfl_up_sync(kFullMask, inc.f, 1);
+      ex.v = shfl_up_acc(inc.v, 1);
+      ex = lane == 0 ? cin : seg_combine(cin, ex);
+      if (first_k >= 0) {
+        Acc<COMP> val = ex.v;  // earlier parts of the row first
+        val.add(first_v);
+        const int r = ra + first_k;
+        if (need_lb && r == rs) {
+          // the range's first row end closes row rs, begun in an earlier
+          // range: finished by the look-back below
+          S.pend = 1;
+          S.pend_s = val.s;
+          S.pend_c = val.comp();
+        } else {
+          float vv = val.value();
+          if (scale) vv *= __ldg(scale + r);
+          a.y[r] = vv;
+        }
+      }
+      carry = shfl_idx_acc(seg_combine(cin, inc).v, 31);
+
+      ra = ra2;
+      lo = lo2;
+      hi = hi2;
+      __syncwarp();  // S.re is rewritten by the next tile
+    }
+    if (__any_sync(kFullMask, bad) && lane == 0) raise_flag(hdr, EL_FLAG_OFFSETS, (unsigned)ra);
+
+    // range end (re, ne): publish the partial of the row still open, if this
+    // range holds any of its nonzeros; exactly one later range reads it
+    const int off_re = __ldg(a.offsets + re);
+    if (lane == 0) {
+      if ((long long)re == a.rows && (long long)off_re != a.nnz)
+        raise_flag(hdr, EL_FLAG_NNZ_MISMATCH, (unsigned)re);
+      if (ne > max(off_re, ns) && g < a.ws.nslots && !(a.test_hooks & 1)) {
+        CarrySlot* sl = a.ws.slots + g;
+        sl->sum = carry.s;
+        sl->comp = carry.comp();
+        st_release_u32(&sl->flag, tag);
+      }
+    }
+    __syncwarp();
+    if (need_lb && S.pend) {
+      // row rs began in range gfirst: sum the partials of ranges [gfirst, g)
+      // in a fixed order
+      const long long gfirst = ((long long)rs + off_rs) / a.range_items;
+      Acc<COMP> acc;
+      bool ok = true;
+      for (long long kk = gfirst + lane; kk < g && kk < a.ws.nslots; kk += 32) {
+        CarrySlot* sl = a.ws.slots + kk;
+        if (ld_acquire_u32(&sl->flag) != tag) {
+          const uint64_t t0 = global_timer_ns();
+          while (ld_acquire_u32(&sl->flag) != tag) {
+            if (global_timer_ns() - t0 > a.wait_ns) {
+              ok = false;
+              break;
+            }
+            __nanosleep(100);
+          }
+        }
+        if (!ok) break;
+        Acc<COMP> pv;
+        pv.set(__ldcg(&sl->sum), __ldcg(&sl->comp));
+        acc.add(pv);
+      }
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) {
+        Acc<COMP> ov = shfl_xor_acc(acc, d);
+        if ((lane & d) == 0) {
+          acc.add(ov);
+        } else {
+          ov.add(acc);
+          acc = ov;
+        }
+      }
+      ok = __all_sync(kFullMask, ok);
+      if (lane == 0) {
+        if (!ok) raise_flag(hdr, EL_FLAG_TIMEOUT, 4);
+        Acc<COMP> pend;
+        pend.set(S.pend_s, S.pend_c);
+        acc.add(pend);
+        float vv = acc.value();
+        if (scale) vv *= __ldg(scale + rs);
+        a.y[rs] = vv;
+      }
+    }
+  }
+
+  // the last warp to finish hands the workspace back for the next launch
+  if (lane == 0) {
+    __threadfence();
+    const unsigned total_warps = gridDim.x * kWarps;
+    const unsigned prev = atomicAdd(&hdr->done, 1u);
+    if (prev == total_warps - 1) finish_launch(hdr, epoch);
+  }
+}
+
+template <typename VT, bool COMP>
+int resident_warps(int device) {
+  const int per_sm =
+      resident_ctas_per_sm((const void*)merge_path_nz_kernel<VT, COMP>, kTPB, 0);
+  return (per_sm > 0 ? per_sm : 1) * kWarps * device_info(device).sm_count;
+}
+
+template <typename VT, bool COMP>
+el_status launch(const SpmvCall& c) {
+  const long long total = c.A.rows + c.A.nnz;
+  // ranges of whole 256-item units, one per resident warp
+  const long long units = (total + kTileNz - 1) / kTileNz;
+  long long W = resident_warps<VT, COMP>(c.device);
+  if (c.o.max_ctas > 0 && (long long)c.o.max_ctas * kWarps < W) W = (long long)c.o.max_ctas * kWarps;
+  if (W > units) W = units;
+  if (W < 1) W = 1;
+  const long long upr = (units + W - 1) / W;
+  Args a;
+  a.rows = c.A.rows;
+  a.cols = c.A.cols;
+  a.nnz = c.A.nnz;
+  a.offsets = c.A.offsets;
+  a.indices = c.A.indices;
+  a.values = c.A.values;
+  a.row_scale = c.A.row_scale;
+  a.x = c.x;
+  a.y = c.y;
+  a.range_items = upr * kTileNz;
+  a.num_ranges = (units + upr - 1) / upr;
+  a.vec_ok = ((uintptr_t)c.A.indices % 16) == 0 && ((uintptr_t)c.A.values % 16) == 0;
+  a.test_hooks = c.o.test_hooks;
+  a.wait_ns = c.wait_ns;
+  a.ws = c.ws;
+  if (a.num_ranges > c.ws.nslots)
+    return fail(EL_ERR_INVALID_ARGUMENT, "merge_path: workspace too small");
+  const long long grid = (a.num_ranges + kWarps - 1) / kWarps;
+  merge_path_nz_kernel<VT, COMP><<<(unsigned)grid, kTPB, 0, c.stream>>>(a);
+  return cuda_status(cudaGetLastError(), "merge_path launch");
+}
+
+template <typename VT, bool COMP>
+long long slots_needed(const SpmvCall& c) {
+  return resident_warps<VT, COMP>(c.device);
+}
+
+}  // namespace mpn
+}  // namespace el

@@ -134,10 +134,16 @@ typedef struct el_spmv_opts {
                                 merge_path ranges skip publishing their row
                                 carries, so a range that needs one waits until
                                 wait_limit_us and reports EL_FLAG_TIMEOUT */
-  int32_t variant;           /* merge_path kernel: 0 = warp-streaming (each
-                                warp walks its own range, register prefetch);
-                                1 = CTA ring (producer warps stream the
-                                range into shared memory with bulk copies) */
+  int32_t variant;           /* merge_path kernel (same results within the
+                                FP32 bound, deterministic):
+                                0 = warp ranges walked in tiles of 256
+                                    nonzeros, 8 per lane, vector loads;
+                                1 = CTA ring: producer warps stream the range
+                                    into shared memory with bulk copies;
+                                2 = warp ranges walked in tiles of 256 merge
+                                    items, lane t from the split point of
+                                    diagonal 8t (the reference's per-thread
+                                    split) */
   int32_t reserved[5];
 } el_spmv_opts;
 
