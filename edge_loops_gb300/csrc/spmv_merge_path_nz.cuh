@@ -51,8 +51,12 @@ struct Args {
   WsView ws;
 };
 
+template <bool COMP>
 struct WarpSmem {
-  int re[kMaxEnds];  // end position (tile-local nonzero index) of each row end
+  int re[kMaxEnds];            // end position (tile-local nonzero index) of each row end
+  float yv[kMaxEnds];          // the tile's row sums, staged for one coalesced store
+  float yc[COMP ? kMaxEnds : 1];
+  unsigned char kp[32][kPer];  // row end closed after lane l's product i (tile-local)
   int pend;
   float pend_s, pend_c;
 };
@@ -97,11 +101,11 @@ __device__ __forceinline__ float ld_val(const VT* p) {
 }
 
 template <typename VT, bool COMP>
-__global__ void __launch_bounds__(kTPB, 4)
+__global__ void __launch_bounds__(kTPB, 3)
     merge_path_nz_kernel(const Args a) {
-  __shared__ WarpSmem smem_all[kWarps];
+  __shared__ WarpSmem<COMP> smem_all[kWarps];
   const int lane = threadIdx.x & 31;
-  WarpSmem& S = smem_all[threadIdx.x >> 5];
+  WarpSmem<COMP>& S = smem_all[threadIdx.x >> 5];
   WsHeader* hdr = a.ws.hdr;
   const VT* vals = reinterpret_cast<const VT*>(a.values);
   const float* __restrict__ scale = a.row_scale;
@@ -161,10 +165,27 @@ __global__ void __launch_bounds__(kTPB, 4)
       return k <= rows ? __ldcs(a.offsets + k) : 0x7fffffff;
     };
 
+    // x at the tile's columns, gathered one tile ahead (a column outside
+    // [0, cols) reads nothing and raises the flag once per range)
+    float xg[kPer];
+    bool bad_col = false;
+    auto gather = [&]() {
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
+        const int col = c[i];
+        xg[i] = 0.f;
+        if ((unsigned)col < cols)
+          xg[i] = __ldg(a.x + col);
+        else if (col != -1)
+          bad_col = true;
+      }
+    };
+
     int ra = rs, lo = ns;  // first row not yet closed; first nonzero of the tile
     int hi = tile_hi(lo);
     load_tile(lo, hi);
     int o = load_ends(ra);
+    gather();
     Acc<COMP> carry;
     bool bad = false;
 
@@ -196,16 +217,7 @@ __global__ void __launch_bounds__(kTPB, 4)
       // products of this lane's nonzeros 8 lane + i
       float p[kPer];
 #pragma unroll
-      for (int i = 0; i < kPer; ++i) {
-        p[i] = 0.f;
-        if (kPer * lane + i < Y) {
-          const int col = c[i];
-          if ((unsigned)col < cols)
-            p[i] = __fmul_rn(v[i], __ldg(a.x + col));
-          else
-            raise_flag(hdr, EL_FLAG_INDEX_RANGE, (unsigned)(lo + kPer * lane + i));
-        }
-      }
+      for (int i = 0; i < kPer; ++i) p[i] = kPer * lane + i < Y ? __fmul_rn(v[i], xg[i]) : 0.f;
       // the window registers are free: start loading the next tile
       const int lo2 = hi, hi2 = tile_hi(hi), ra2 = ra + X;
       if (lo2 < ne) load_tile(lo2, hi2);
@@ -225,37 +237,42 @@ __global__ void __launch_bounds__(kTPB, 4)
       int kend = __shfl_down_sync(kFullMask, k, 1);
       if (lane == 31) kend = X;
 
-      Acc<COMP> run, first_v;
-      int first_k = -1;
-      int nxt = k < kend ? S.re[k] - kPer * lane : 0x7fffffff;
-      auto close_row = [&]() {
-        if (first_k < 0) {
-          first_k = k;
-          first_v = run;
-        } else {
-          const int r = ra + k;
-          float val = run.value();
-          if (scale) val *= __ldg(scale + r);
-          a.y[r] = val;
+      // rows of the tile start at 0 (an empty row stays 0); the lane's row
+      // ends become "close after product i" bits (the first end at each
+      // position closes the running sum, further ends there are empty rows)
+      for (int kk = lane; kk < X; kk += 32) {
+        S.yv[kk] = 0.f;
+        if (COMP) S.yc[kk] = 0.f;
+      }
+      unsigned mask = 0;
+      for (int kk = k; kk < kend; ++kk) {
+        const int q = S.re[kk] - kPer * lane;
+        if (q >= 1 && q <= kPer) {
+          if (kk == k || S.re[kk - 1] != S.re[kk]) {
+            mask |= 1u << (q - 1);
+            S.kp[lane][q - 1] = (unsigned char)kk;
+          }
+        } else if (q != 0 || lane != 0) {
+          bad = true;  // an end outside the lane's nonzeros: malformed offsets
         }
-        run = Acc<COMP>();
-        ++k;
-        nxt = k < kend ? S.re[k] - kPer * lane : 0x7fffffff;
-      };
-      while (nxt <= 0) close_row();
+      }
+      __syncwarp();
+      Acc<COMP> run;
 #pragma unroll
       for (int i = 0; i < kPer; ++i) {
         run.add(p[i]);
-        while (nxt == i + 1) close_row();
+        if ((mask >> i) & 1u) {
+          const int kk = S.kp[lane][i];
+          S.yv[kk] = run.s;
+          if (COMP) S.yc[kk] = run.comp();
+          run = Acc<COMP>();
+        }
       }
-      if (k < kend) {  // ends beyond the lane's nonzeros: malformed offsets
-        bad = true;
-        while (k < kend) close_row();
-      }
+      const bool has_end = kend > k;  // the lane closes row ra + k first
 
       // stitch rows across lanes; lane 0 continues the previous tile's row
       SegVal<COMP> mine, cin;
-      mine.f = first_k >= 0;
+      mine.f = has_end;
       mine.v = run;
       cin.f = 0;
       cin.v = carry;
@@ -264,29 +281,39 @@ __global__ void __launch_bounds__(kTPB, 4)
       ex.f = __shfl_up_sync(kFullMask, inc.f, 1);
       ex.v = shfl_up_acc(inc.v, 1);
       ex = lane == 0 ? cin : seg_combine(cin, ex);
-      if (first_k >= 0) {
+      if (has_end) {
         Acc<COMP> val = ex.v;  // earlier parts of the row first
-        val.add(first_v);
-        const int r = ra + first_k;
-        if (need_lb && r == rs) {
+        Acc<COMP> mine_part;
+        mine_part.set(S.yv[k], COMP ? S.yc[k] : 0.f);
+        val.add(mine_part);
+        if (need_lb && ra + k == rs) {
           // the range's first row end closes row rs, begun in an earlier
           // range: finished by the look-back below
           S.pend = 1;
           S.pend_s = val.s;
           S.pend_c = val.comp();
-        } else {
-          float vv = val.value();
-          if (scale) vv *= __ldg(scale + r);
-          a.y[r] = vv;
         }
+        S.yv[k] = val.s;
+        if (COMP) S.yc[k] = val.comp();
+      }
+      __syncwarp();
+      for (int kk = lane; kk < X; kk += 32) {  // coalesced store of the tile's rows
+        const int r = ra + kk;
+        if (need_lb && r == rs) continue;
+        float vv = COMP ? __fadd_rn(S.yv[kk], S.yc[kk]) : S.yv[kk];
+        if (scale) vv *= __ldg(scale + r);
+        a.y[r] = vv;
       }
       carry = shfl_idx_acc(seg_combine(cin, inc).v, 31);
 
       ra = ra2;
       lo = lo2;
       hi = hi2;
+      if (lo < ne) gather();  // the next tile's window has arrived by now
       __syncwarp();  // S.re is rewritten by the next tile
     }
+    if (__any_sync(kFullMask, bad_col) && lane == 0)
+      raise_flag(hdr, EL_FLAG_INDEX_RANGE, (unsigned)ra);
     if (__any_sync(kFullMask, bad) && lane == 0) raise_flag(hdr, EL_FLAG_OFFSETS, (unsigned)ra);
 
     // range end (re, ne): publish the partial of the row still open, if this
