@@ -121,7 +121,11 @@ SIGNATURES = {
                                      C.POINTER(C.c_int32)]),
     "el_batch_plan_errors": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint32), C.c_int]),
     "el_batch_plan_destroy": (C.c_int, [C.c_void_p]),
+    "el_spmv_static_scratch": (C.c_int, [C.POINTER(ElCsr), C.c_void_p, C.c_void_p, C.c_int32,
+                                         C.POINTER(C.c_uint32), C.c_void_p]),
 }
+
+EL_STATIC_MAX_RANGES = 4096
 
 _lib = None
 

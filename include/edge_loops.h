@@ -265,6 +265,38 @@ el_status el_batch_plan_errors(el_batch_plan* plan, el_stream_t stream,
                                uint32_t* flags, int clear);
 el_status el_batch_plan_destroy(el_batch_plan* plan);
 
+/* ---- SpMV without device allocation (no counterpart in the reference) --
+ * y = A x with the default merge-path kernel, for callers that may not
+ * allocate device memory once they are running: processes whose device
+ * memory is all reserved up front by their own allocator (inference
+ * servers, frameworks with a caching allocator, where a cudaMalloc would
+ * fail or bypass the budget), real-time loops that forbid allocation (and
+ * the device-wide synchronisation cudaMalloc/cudaFree bring) after start-up,
+ * and plugins hosted by an application that owns the device allocator.
+ * Every other entry point may allocate a workspace on first use; this one
+ * never calls cudaMalloc, cudaFree or any allocating routine.
+ *
+ * Its scratch (range tickets, error flags and one carry slot per warp
+ * range) is a fixed array in the library's device image: 64 KiB + 64 B,
+ * present on every GPU that loads the library until the process exits.
+ * The first call on a device looks the array's device address up
+ * (cudaGetSymbolAddress), so make that first call before any stream
+ * capture.  All calls on a device share the array: calls that may overlap
+ * on the GPU (other streams, other host threads) race and give wrong
+ * results; serialise them.  Each call clears the array's counters and
+ * flags itself.
+ *
+ * num_ranges: warp ranges the work is split into, 0 = one per resident
+ * warp (at most EL_STATIC_MAX_RANGES); a larger value is rejected with
+ * EL_ERR_INVALID_ARGUMENT.  With flags != NULL the call synchronises
+ * `stream`, stores the EL_FLAG_* bits the kernel raised and returns
+ * EL_ERR_DEVICE if any is set; with flags == NULL it is asynchronous.
+ * Values FP32 / BF16 / FP16 with optional row scales; FP32 accumulation. */
+#define EL_STATIC_MAX_RANGES 4096
+el_status el_spmv_static_scratch(const el_csr* A, const float* x, float* y,
+                                 int32_t num_ranges, uint32_t* flags,
+                                 el_stream_t stream);
+
 /* ---- mixed precision -------------------------------------------------- */
 /* Converts FP32 values to BF16 / FP16 (round to nearest even).  With
  * row_scale != NULL, each row is first divided by a power of two chosen so
