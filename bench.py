@@ -432,6 +432,193 @@ def run_reference(args, rank, world):
     }
 
 
+# ------------------------------------------------------ SpMM and batched SpMV
+def _time_device(step, steps, warmup, flush, stream):
+    """Mean CUDA-event time (ms) of step() over `steps` runs, L2 flushed
+    before each run outside the timed interval."""
+    import torch
+    for _ in range(warmup):
+        flush.fill_(1.0)
+        step()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for k in range(steps):
+        flush.fill_(float(k))
+        starts[k].record(stream)
+        step()
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / steps
+
+
+def run_spmm(args):
+    """SpMM C = A B (BASELINE config 4): A power-law 2^20 x 2^20 with ~8M
+    nonzeros (Zipf 2.0, cap 100000, seed 3), B dense row-major 2^20 x n."""
+    import numpy as np
+    import torch
+    import oracle
+    from edge_loops_gb300 import api, synth
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    off, idx, vals, x, cols = synth.power_law(rows=1 << 20, target_nnz=8_000_000, exponent=2.0,
+                                              cap=100_000, seed=3, device=dev)
+    A = api.CSR(off, idx, vals, off.numel() - 1, cols)
+    g = torch.Generator(device=dev)
+    g.manual_seed(33)
+    B = torch.rand(cols, args.n, generator=g, device=dev) * 2 - 1
+    bdt = {"f32": torch.float32, "bf16": torch.bfloat16, "f16": torch.float16}[args.b_dtype]
+    B = B.to(bdt)
+    Cm = torch.empty(A.rows, args.n, device=dev)
+    sb = B.element_size()
+    compulsory = A.nnz * 8 + 4 * (A.rows + 1) + cols * args.n * sb + A.rows * args.n * 4
+    gather = A.nnz * 8 + 4 * (A.rows + 1) + A.nnz * args.n * sb + A.rows * args.n * 4
+    ws = api.Workspace()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, device=dev)
+    ms = _time_device(lambda: api.spmm(A, B, Cm, schedule=args.schedule, workspace=ws),
+                      args.steps, args.warmup, flush, torch.cuda.current_stream())
+    if ws.errors():
+        raise SystemExit("device error flags in SpMM")
+    # parity on a sample of 2048 rows: FP64 oracle of those rows
+    rng = np.random.default_rng(0)
+    rows_s = np.sort(rng.choice(A.rows, 2048, replace=False))
+    offh, idxh, valh = off.cpu().numpy(), idx.cpu().numpy(), vals.cpu().numpy()
+    lens = offh[rows_s + 1] - offh[rows_s]
+    so = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    sel = np.concatenate([np.arange(offh[r], offh[r + 1]) for r in rows_s])
+    Bh = B.float().cpu().numpy()
+    C64, Ca = oracle.spmm_f64(so, idxh[sel], valh[sel], Bh)
+    got = Cm[torch.as_tensor(rows_s, device=dev)].cpu().numpy().astype(np.float64)
+    u = 2.0 ** -24
+    nn = (np.diff(so.astype(np.int64)) + 2)[:, None]
+    bad = int(np.sum(np.abs(got - C64) > (nn * u / (1 - nn * u)) * Ca))
+    if bad:
+        raise SystemExit(f"SpMM output fails the oracle bound in {bad} entries")
+    peak, kind = measured_peaks()
+    ach = compulsory / (ms * 1e-3) / 1e9
+    return {
+        "metric": "SpMM achieved bandwidth (compulsory bytes / kernel time)",
+        "value": round(ach, 2), "unit": "GB/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": f"f32 values, {args.b_dtype} B, f32 accumulate",
+        "data": "synthetic (seeded generator; SuiteSparse not available)",
+        "config": {"workload": "SpMM power-law 2^20 x 2^20 ~8M nnz (Zipf 2.0, cap 1e5, seed 3),"
+                               f" B 2^20 x {args.n} {args.b_dtype}",
+                   "schedule": args.schedule, "n": args.n, "nnz": A.nnz,
+                   "compulsory_bytes": compulsory, "gather_model_bytes": gather,
+                   "l2": "flushed before every step (512 MiB write, outside the timed kernel)"},
+        "roofline": {"bound": "hbm", "achieved": round(ach, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(ach / peak, 4), "peak_source": kind,
+                     "achieved_gather_model": round(gather / (ms * 1e-3) / 1e9, 2),
+                     "traffic": None},
+        "gpu_launches": args.steps * ((args.n + 127) // 128),
+        "check": {"sampled_rows": 2048, "entries_outside_fp32_bound": 0},
+    }
+
+
+def run_batched(args):
+    """Batched SpMV (BASELINE config 5): 4096 square CSRs, rows log-uniform in
+    [64, 65536], log-normal row lengths (mean 8, sigma 1), seed 4; one
+    persistent launch replayed from a CUDA graph.  Also times the plain FP32
+    merge-path kernel launched once per matrix (the comparison the target is
+    defined against) and the batched FP32 plan."""
+    import numpy as np
+    import torch
+    import oracle
+    from edge_loops_gb300 import api, synth
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    R, offc, idxc, valc, xc, rs, ns = synth.batched(count=4096, seed=4, device=dev)
+    items32, y32 = api.batched_items(R, offc, idxc, valc, xc, rs, ns)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, device=dev)
+
+    def total_bytes(items, vb, scaled):
+        return sum(synth.algorithmic_bytes(A.rows, A.cols, A.nnz, vb, row_scale=scaled)
+                   for A, _, _ in items)
+
+    b32 = total_bytes(items32, 4, False)
+    plan32 = api.BatchPlan(items32)
+    ms32 = _time_device(plan32.execute, args.steps, args.warmup, flush, stream)
+    if args.value_dtype == "f32":
+        items, plan, ms, nb = items32, plan32, ms32, b32
+    else:
+        tdt = torch.bfloat16 if args.value_dtype == "bf16" else torch.float16
+        yq = torch.empty_like(y32)
+        items = [(A.quantized(tdt, per_row_scale=True), x, yq[int(rs[m]): int(rs[m]) + A.rows])
+                 for m, (A, x, _) in enumerate(items32)]
+        plan = api.BatchPlan(items)
+        ms = _time_device(plan.execute, args.steps, args.warmup, flush, stream)
+        nb = total_bytes(items, 2, True)
+    if plan.errors() or plan32.errors():
+        raise SystemExit("device error flags in the batched plan")
+    # plain FP32 kernel, one launch per matrix
+    ws = api.Workspace()
+
+    def per_matrix():
+        for A, x, y in items32:
+            api.spmv(A, x, y, schedule="merge_path_flat", workspace=ws)
+
+    per_steps = max(3, min(args.steps, 10))
+    per_matrix()  # sizes the workspace before capture
+    ms_plain_eager = _time_device(per_matrix, per_steps, 2, flush, stream)
+    # the same 4096 launches captured in one CUDA graph (no host overhead):
+    # the stricter comparison
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        per_matrix()
+    ms_plain = _time_device(graph.replay, args.steps, args.warmup, flush, stream)
+    plan32.execute()
+    plan.execute()
+    torch.cuda.synchronize()
+    # parity: 512 sampled matrices against FP64 of the FP32 matrices
+    rng = np.random.default_rng(1)
+    worst, outside = 0.0, 0
+    for m in rng.choice(len(items), 512, replace=False):
+        A32, x, _ = items32[m]
+        A, _, y = items[m]
+        off = A32.offsets.cpu().numpy()
+        y64, yabs = oracle.spmv_f64(off, A32.indices.cpu().numpy(), A32.values.cpu().numpy(),
+                                    x.cpu().numpy())
+        yy = y.cpu().numpy().astype(np.float64)
+        worst = max(worst, oracle.error_metrics(yy, y64, yabs)[0])
+        if args.value_dtype == "f32":
+            u = 2.0 ** -24
+            n = np.diff(off.astype(np.int64)) + 2
+            outside += int(np.sum(np.abs(yy - y64) > (n * u / (1 - n * u)) * yabs))
+    if outside or worst > 1e-2:
+        raise SystemExit(f"batched output check failed: {outside} rows, max rel err {worst}")
+    peak, kind = measured_peaks()
+    ach = nb / (ms * 1e-3) / 1e9
+    thr = lambda b, t: b / (t * 1e-3) / 1e9  # noqa: E731
+    return {
+        "metric": "batched SpMV achieved bandwidth (algorithmic bytes / graph time)",
+        "value": round(ach, 2), "unit": "GB/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": f"{args.value_dtype} values, f32 accumulate",
+        "data": "synthetic (seeded generator; SuiteSparse not available)",
+        "config": {"workload": "4096 square CSRs, rows log-uniform [64, 65536], log-normal "
+                               "nnz/row (mean 8, sigma 1), seed 4",
+                   "rows_total": int(R.sum()), "nnz_total": int(idxc.numel()),
+                   "algorithmic_bytes_per_step": nb, "plan": plan.info(),
+                   "l2": "flushed before every step (512 MiB write, outside the timed graph)"},
+        "roofline": {"bound": "hbm", "achieved": round(ach, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(ach / peak, 4), "peak_source": kind, "traffic": None},
+        "comparison": {
+            "batched_fp32_GBps": round(thr(b32, ms32), 2), "batched_fp32_ms": round(ms32, 4),
+            "plain_fp32_per_matrix_graph_GBps": round(thr(b32, ms_plain), 2),
+            "plain_fp32_per_matrix_graph_ms": round(ms_plain, 4),
+            "plain_fp32_per_matrix_eager_ms": round(ms_plain_eager, 4),
+            "speedup_vs_plain_fp32_per_matrix_graph": round(ms_plain / ms, 3),
+            "speedup_vs_plain_fp32_per_matrix_eager": round(ms_plain_eager / ms, 3),
+            "speedup_vs_batched_fp32": round(ms32 / ms, 3),
+            "max_rel_err_vs_fp64_of_fp32_matrices": worst},
+        "gpu_launches": args.steps,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -445,6 +632,8 @@ def main():
     ap.add_argument("--variant", type=int, default=0,
                     help="merge_path kernel: 0 warp-streaming, 1 CTA ring")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--n", type=int, default=128, help="SpMM: columns of B")
+    ap.add_argument("--b-dtype", default="f32", choices=["f32", "bf16", "f16"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -466,6 +655,11 @@ def main():
     if world > 1:
         torch.distributed.init_process_group(
             "nccl", device_id=torch.device("cuda", _env_int("LOCAL_RANK", 0)))
+    if args.workload in ("spmm_powerlaw", "spmv_batched"):
+        line = run_spmm(args) if args.workload == "spmm_powerlaw" else run_batched(args)
+        if rank == 0:
+            print(json.dumps(line))
+        return
     line = run_ours(args, rank, world)
     if rank == 0:
         print(json.dumps(line))
