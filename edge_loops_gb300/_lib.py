@@ -75,6 +75,7 @@ EL_BATCH_LEN_BUCKETS = 11
 EL_BATCH_CV_BUCKETS = 4
 EL_BATCH_TABLE_SIZE = EL_BATCH_ROW_BUCKETS * EL_BATCH_LEN_BUCKETS * EL_BATCH_CV_BUCKETS
 EL_BATCH_MAX_ROW_NNZ = 16384
+EL_BATCH_NZ_WALK = 64
 
 
 class ElBatchOpts(C.Structure):

@@ -290,12 +290,13 @@ class BatchPlan:
 
     def info(self):
         w = C.c_int64()
-        t = (C.c_int32 * 6)()
+        t = (C.c_int32 * 7)()
         hv = C.c_int32()
         L.check(L.lib().el_batch_plan_info(self.handle, C.byref(w), t, C.byref(hv)),
                 "el_batch_plan_info")
         return {"work_items": int(w.value),
                 "matrices_by_threads_per_row": {1 << i: int(t[i]) for i in range(6)},
+                "matrices_nz_walk": int(t[6]),
                 "heavy_matrices": int(hv.value)}
 
     def errors(self, clear=True, stream=None):

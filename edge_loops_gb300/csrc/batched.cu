@@ -3,20 +3,24 @@
 //
 // Plan creation: one statistics kernel reads every matrix's row offsets
 // (rows, nonzeros, max row length, sum of squared lengths); the host maps
-// each matrix to a (threads per row, nonzeros per work item) pair -- from the
-// tuning table bucket of (rows, mean row length, coefficient of variation) or
-// the built-in rule -- cuts the matrix into row chunks of about that many
-// nonzeros and uploads the work list.  Execution: a persistent grid strides
-// over the work list; each CTA processes its chunk's rows with TPR lanes per
-// row (the thread_mapped schedule generalised to TPR lanes, a fixed xor-tree
-// reduction, no atomics: deterministic).  Chunks hold whole rows, so no
-// partial sums cross CTAs.
+// each matrix to a (kernel mode, work-item size) pair -- from the tuning
+// table bucket of (rows, mean row length, coefficient of variation) or the
+// built-in rule -- and a split kernel cuts every matrix into work items of
+// whole rows at merge-path diagonals k * 2^chunk (so every item holds about
+// 2^chunk rows + nonzeros).  Execution: a persistent grid whose warps stride
+// over the work list; a warp runs its item either with the nonzero-tiled
+// walk of the merge-path kernel (tiles of 256 nonzeros, 8 per lane, row
+// ends from the offsets window) or with TPR lanes per row (the
+// thread_mapped schedule generalised to TPR lanes with a fixed xor-tree
+// reduction).  Items hold whole rows, so no partial sums cross warps; no
+// atomics: deterministic.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "el_internal.h"
+#include "spmv_merge_path_nz.cuh"
 
 namespace el {
 namespace batch {
@@ -31,15 +35,17 @@ struct Desc {  // one matrix, device side
   int rows;
   int cols;
   int nnz;
-  int pad;
+  int ph;  // tile phase of the nonzero-tiled walk, -1: no 128-bit loads
 };
 
-struct Item {  // rows [r0, r1) of matrix m with TPR = 1 << tpr_log2
+struct Item {  // rows [r0, r1) of matrix m, run in `mode`
   int m;
   int r0;
   int r1;
-  int tpr_log2;
+  int mode;  // 0..5: 1 << mode lanes per row; kNzWalk: nonzero-tiled walk
 };
+
+constexpr int kNzWalk = 6;
 
 struct Stats {
   double sum_sq;
@@ -89,14 +95,11 @@ __global__ void stats_kernel(const Desc* __restrict__ d, Stats* __restrict__ out
 }
 
 template <typename VT, int TPR>
-__device__ __forceinline__ void rows_tpr(const Desc& d, int r0, int r1, WsHeader* hdr) {
-  const int lane = threadIdx.x & 31;
+__device__ __forceinline__ void rows_tpr(const Desc& d, int r0, int r1, int lane, WsHeader* hdr) {
   const int sub = lane % TPR;
   constexpr int RPW = 32 / TPR;
-  const int warp = threadIdx.x >> 5;
-  const int nw = blockDim.x >> 5;
   const VT* vals = reinterpret_cast<const VT*>(d.values);
-  for (int base = r0 + warp * RPW; base < r1; base += nw * RPW) {  // warp-uniform
+  for (int base = r0; base < r1; base += RPW) {  // warp-uniform
     const int row = base + lane / TPR;
     float acc = 0.f;
     if (row < r1) {
@@ -120,22 +123,64 @@ __device__ __forceinline__ void rows_tpr(const Desc& d, int r0, int r1, WsHeader
   }
 }
 
+// Rows [r0, r1) by the nonzero-tiled walk (whole rows: nothing is carried
+// out of the item).  Offsets are clamped, so any content stays in bounds.
 template <typename VT>
-__global__ void __launch_bounds__(256)
+__device__ __forceinline__ void rows_nz(const Desc& d, int r0, int r1, int lane,
+                                        mpn::WarpSmem<false>& S, bool& bad, bool& bad_col) {
+  const int ns = min(max(__ldg(d.offsets + r0), 0), d.nnz);
+  const int ne = min(max(__ldg(d.offsets + r1), ns), d.nnz);
+  const mpn::Src m{d.offsets, d.indices, d.values, d.row_scale, d.x, d.y,
+                   d.rows,    (unsigned)d.cols, d.ph >= 0 ? 1 : 0, d.ph >= 0 ? d.ph : 0};
+  int ra = r0;
+  (void)mpn::walk_rows<VT, false>(m, S, lane, r0, r1, ns, ne, false, bad, bad_col, ra);
+}
+
+template <typename VT>
+__global__ void __launch_bounds__(256, 3)
     batched_spmv_kernel(const Desc* __restrict__ descs, const Item* __restrict__ items,
                         long long n_items, WsHeader* hdr) {
-  for (long long it = blockIdx.x; it < n_items; it += gridDim.x) {  // block-uniform
+  __shared__ mpn::WarpSmem<false> smem[8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  bool bad = false, bad_col = false;
+  const long long stride = (long long)gridDim.x * 8;
+  for (long long it = (long long)blockIdx.x * 8 + warp; it < n_items; it += stride) {  // warp-uniform
     const Item w = items[it];
     const Desc d = descs[w.m];
-    switch (w.tpr_log2) {
-      case 0: rows_tpr<VT, 1>(d, w.r0, w.r1, hdr); break;
-      case 1: rows_tpr<VT, 2>(d, w.r0, w.r1, hdr); break;
-      case 2: rows_tpr<VT, 4>(d, w.r0, w.r1, hdr); break;
-      case 3: rows_tpr<VT, 8>(d, w.r0, w.r1, hdr); break;
-      case 4: rows_tpr<VT, 16>(d, w.r0, w.r1, hdr); break;
-      default: rows_tpr<VT, 32>(d, w.r0, w.r1, hdr); break;
+    switch (w.mode) {
+      case 0: rows_tpr<VT, 1>(d, w.r0, w.r1, lane, hdr); break;
+      case 1: rows_tpr<VT, 2>(d, w.r0, w.r1, lane, hdr); break;
+      case 2: rows_tpr<VT, 4>(d, w.r0, w.r1, lane, hdr); break;
+      case 3: rows_tpr<VT, 8>(d, w.r0, w.r1, lane, hdr); break;
+      case 4: rows_tpr<VT, 16>(d, w.r0, w.r1, lane, hdr); break;
+      case 5: rows_tpr<VT, 32>(d, w.r0, w.r1, lane, hdr); break;
+      default: rows_nz<VT>(d, w.r0, w.r1, lane, smem[warp], bad, bad_col); break;
     }
   }
+  if (__any_sync(kFullMask, bad_col) && lane == 0) raise_flag(hdr, EL_FLAG_INDEX_RANGE, 0);
+  if (__any_sync(kFullMask, bad) && lane == 0) raise_flag(hdr, EL_FLAG_OFFSETS, 0);
+}
+
+// Work items: item i arrives as {m, k, chunk_log2, mode} and leaves as
+// {m, r0, r1, mode} with rows [r0, r1) = the rows whose end falls in merge
+// diagonals [k << chunk, (k + 1) << chunk) of matrix m.
+__global__ void split_kernel(const Desc* __restrict__ descs, Item* __restrict__ items,
+                             long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Item w = items[i];
+  const Desc d = descs[w.m];
+  const long long total = (long long)d.rows + d.nnz;
+  const long long d0 = (long long)w.r0 << w.r1;
+  long long d1 = d0 + (1LL << w.r1);
+  if (d1 > total) d1 = total;
+  const int* row_end = d.offsets + 1;
+  auto a = [&](long long k) { return __ldg(row_end + k); };
+  const long long x0 = seq_merge_search(a, d.rows, 0, d.nnz, d0 < total ? d0 : total);
+  const long long x1 = d1 >= total ? d.rows : seq_merge_search(a, d.rows, 0, d.nnz, d1);
+  w.r0 = (int)min(x0, (long long)d.rows);
+  w.r1 = (int)min(max(x1, x0), (long long)d.rows);
+  items[i] = w;
 }
 
 int row_bucket(long long rows) {
@@ -151,15 +196,20 @@ int len_bucket(double avg) {
 }
 int cv_bucket(double cv) { return cv < 0.25 ? 0 : cv < 0.75 ? 1 : cv < 1.5 ? 2 : 3; }
 
-// Built-in rule (used where the table has no entry): about as many lanes
-// per row as the mean row length, doubled for very uneven rows; 8192
-// nonzeros per work item.
-void builtin_rule(double avg, double cv, int* tpr_log2, int* chunk_log2) {
-  int t = 0;
-  while (t < 5 && (double)(2 << t) <= avg) ++t;
-  if (cv >= 1.5 && t < 5) ++t;
-  *tpr_log2 = t;
-  *chunk_log2 = 13;
+// Kernel mode of a threads-per-row value: 1..32 lanes per row (rounded up
+// to a power of two), EL_BATCH_NZ_WALK: the nonzero-tiled walk.
+int mode_of(int tpr) {
+  if (tpr >= EL_BATCH_NZ_WALK) return kNzWalk;
+  int l2 = 0;
+  while ((1 << l2) < tpr && l2 < 5) ++l2;
+  return l2;
+}
+
+// Built-in rule (used where the table has no entry): the nonzero-tiled
+// walk with work items of 2^12 rows + nonzeros.
+void builtin_rule(double, double, int* mode, int* chunk_log2) {
+  *mode = kNzWalk;
+  *chunk_log2 = 12;
 }
 
 }  // namespace batch
@@ -173,7 +223,7 @@ struct el_batch_plan {
   void* d_items;
   long long n_items;
   int grid;
-  int tpr_counts[6];
+  int tpr_counts[7];
   std::vector<int> heavy;  // matrices run as separate merge-path launches
   std::vector<el_batch_item> items;
   el_workspace* ws;
@@ -233,9 +283,11 @@ el_status el_batch_plan_create(const el_batch_item* items, int32_t count,
   el_batch_opts o;
   el_batch_opts_default(&o);
   if (opts) o = *opts;
-  if (o.force_threads_per_row < 0 || o.force_threads_per_row > 32 ||
+  if (o.force_threads_per_row < 0 ||
+      (o.force_threads_per_row > 32 && o.force_threads_per_row != EL_BATCH_NZ_WALK) ||
       (o.force_threads_per_row & (o.force_threads_per_row - 1)) != 0)
-    return fail(EL_ERR_INVALID_ARGUMENT, "force_threads_per_row must be a power of two <= 32");
+    return fail(EL_ERR_INVALID_ARGUMENT,
+                "force_threads_per_row must be a power of two <= 32 or EL_BATCH_NZ_WALK");
   int dtype = count > 0 ? items[0].A.value_dtype : EL_F32;
   for (int i = 0; i < count; ++i) {
     const el_csr& A = items[i].A;
@@ -277,8 +329,10 @@ el_status el_batch_plan_create(const el_batch_item* items, int32_t count,
   std::vector<batch::Desc> descs(count);
   for (int i = 0; i < count; ++i) {
     const el_batch_item& b = items[i];
+    int vec_ok = 0, ph = 0;
+    mpn::tile_phase(b.A.indices, b.A.values, b.A.value_dtype == EL_F32 ? 4 : 2, &vec_ok, &ph);
     descs[i] = batch::Desc{b.A.offsets, b.A.indices, b.A.values, b.A.row_scale, b.x, b.y,
-                           (int)b.A.rows, (int)b.A.cols, (int)b.A.nnz, 0};
+                           (int)b.A.rows, (int)b.A.cols, (int)b.A.nnz, vec_ok ? ph : -1};
   }
   std::vector<batch::Stats> stats(count);
   if (count > 0) {
@@ -316,32 +370,24 @@ el_status el_batch_plan_create(const el_batch_item* items, int32_t count,
     const double avg = (double)A.nnz / rows;
     const double var = std::max(0.0, stats[i].sum_sq / rows - avg * avg);
     const double cv = avg > 0 ? std::sqrt(var) / avg : 0.0;
-    int tl = 0, cl = 13;
-    batch::builtin_rule(avg, cv, &tl, &cl);
+    int mode = batch::kNzWalk, cl = 12;
+    batch::builtin_rule(avg, cv, &mode, &cl);
     if (o.table) {
       const int idx = (batch::row_bucket(A.rows) * EL_BATCH_LEN_BUCKETS + batch::len_bucket(avg)) *
                           EL_BATCH_CV_BUCKETS + batch::cv_bucket(cv);
       const int ent = o.table[idx];
       if (ent > 0) {
-        int t = ent & 0xff, l2 = 0;
-        while ((1 << l2) < t && l2 < 5) ++l2;
-        tl = l2;
+        mode = batch::mode_of(ent & 0xff);
         cl = (ent >> 8) & 0xff;
       }
     }
-    if (o.force_threads_per_row > 0) {
-      int l2 = 0;
-      while ((1 << l2) < o.force_threads_per_row) ++l2;
-      tl = l2;
-    }
+    if (o.force_threads_per_row > 0) mode = batch::mode_of(o.force_threads_per_row);
     if (o.force_chunk_log2 > 0) cl = o.force_chunk_log2;
     cl = std::min(std::max(cl, 6), 24);
-    p->tpr_counts[tl]++;
-    long long rows_per = (long long)std::llround((double)(1LL << cl) / std::max(avg, 1.0));
-    // at least one row for every lane group of the CTA
-    rows_per = std::max(rows_per, (long long)(256 >> tl));
-    for (long long r = 0; r < A.rows; r += rows_per)
-      work.push_back(batch::Item{i, (int)r, (int)std::min<long long>(A.rows, r + rows_per), tl});
+    p->tpr_counts[mode]++;
+    const long long total = (long long)A.rows + A.nnz;
+    const long long nk = (total + (1LL << cl) - 1) >> cl;
+    for (long long k = 0; k < nk; ++k) work.push_back(batch::Item{i, (int)k, cl, mode});
   }
   p->n_items = (long long)work.size();
   if (p->n_items > 0) {
@@ -349,8 +395,14 @@ el_status el_batch_plan_create(const el_batch_item* items, int32_t count,
     if (e != cudaSuccess) return bail(cuda_status(e, "batch work list"));
     e = cudaMemcpyAsync(p->d_items, work.data(), sizeof(batch::Item) * work.size(),
                         cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+      batch::split_kernel<<<(unsigned)((p->n_items + 255) / 256), 256, 0, s>>>(
+          reinterpret_cast<const batch::Desc*>(p->d_descs),
+          reinterpret_cast<batch::Item*>(p->d_items), p->n_items);
+      e = cudaGetLastError();
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return bail(cuda_status(e, "batch work list upload"));
+    if (e != cudaSuccess) return bail(cuda_status(e, "batch work list"));
   }
   const int per_sm = resident_ctas_per_sm(
       dtype == EL_F32 ? (const void*)batch::batched_spmv_kernel<float>
@@ -407,7 +459,7 @@ el_status el_batch_plan_info(const el_batch_plan* p, int64_t* work_items,
   if (!p) return fail(EL_ERR_NULL_POINTER, "plan is NULL");
   if (work_items) *work_items = p->n_items;
   if (tpr_counts)
-    for (int i = 0; i < 6; ++i) tpr_counts[i] = p->tpr_counts[i];
+    for (int i = 0; i < 7; ++i) tpr_counts[i] = p->tpr_counts[i];
   if (heavy) *heavy = (int32_t)p->heavy.size();
   return EL_OK;
 }

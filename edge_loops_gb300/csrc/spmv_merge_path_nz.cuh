@@ -45,7 +45,8 @@ struct Args {
   float* y;
   long long range_items;  // merge items per warp range
   long long num_ranges;
-  int vec_ok;             // indices and values 16-byte aligned
+  int vec_ok;             // 128-bit loads allowed at tile starts (tile_phase)
+  int ph;                 // tile phase (tile_phase)
   int test_hooks;
   unsigned long long wait_ns;
   WsView ws;
@@ -100,6 +101,287 @@ __device__ __forceinline__ float ld_val(const VT* p) {
   return to_f32(*p);
 }
 
+// One matrix as the tile walk sees it.
+struct Src {
+  const int* offsets;
+  const int* indices;
+  const void* values;
+  const float* row_scale;
+  const float* x;
+  float* y;
+  int rows;
+  unsigned cols;
+  int vec_ok;  // 128-bit loads allowed at tile starts
+  int ph;      // tiles start where (nonzero index + ph) is a multiple of kTileNz
+};
+
+// 128-bit loads of indices and values need both arrays at the same phase
+// modulo 8 elements (indices 4-byte, values element-aligned); tiles then
+// start on 32-byte boundaries of both.  Otherwise every load is scalar.
+inline void tile_phase(const void* indices, const void* values, int vbytes, int* vec_ok,
+                       int* ph) {
+  const uintptr_t ia = (uintptr_t)indices, va = (uintptr_t)values;
+  const bool ok = ia % 4 == 0 && va % (uintptr_t)vbytes == 0 &&
+                  ((ia / 4) - (va / (uintptr_t)vbytes)) % 8 == 0;
+  *vec_ok = ok ? 1 : 0;
+  *ph = ok ? (int)((ia / 4) % kTileNz) : 0;
+}
+
+// The warp walks the merge range from (rs, ns) to (re, ne): rows [rs, re)
+// end inside it and are written to y (row rs only when it begins in the
+// range, i.e. !need_lb; otherwise its partial is left in S.pend*), and the
+// partial sum of the row still open at the end (row re's nonzeros [.., ne))
+// is returned.  Sets bad / bad_col on malformed input; ra_out = the first
+// row not closed.
+template <typename VT, bool COMP>
+__device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, const int lane,
+                                               const int rs, const int re, const int ns,
+                                               const int ne, const bool need_lb, bool& bad,
+                                               bool& bad_col, int& ra_out) {
+  const VT* vals = reinterpret_cast<const VT*>(m.values);
+  const float* __restrict__ scale = m.row_scale;
+  const int rows = m.rows;
+  const unsigned cols = m.cols;
+
+  // tile [lo, hi): nonzeros up to the next multiple of kTileNz (or ne)
+  auto tile_hi = [&](int l) -> int {
+    if (l >= ne) return l;
+    const long long t = (((long long)l + m.ph) & ~(long long)(kTileNz - 1)) + kTileNz - m.ph;
+    return t < ne ? (int)t : ne;
+  };
+  int c[kPer];
+  float v[kPer];
+  auto load_tile = [&](int l, int h) {
+    const int j0 = l + kPer * lane;
+    if (m.vec_ok && h - l == kTileNz && ((l + m.ph) & 7) == 0) {
+      load8i(m.indices + j0, c);
+      load8(vals + j0, v);
+    } else {
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
+        const int j = j0 + i;
+        if (j < h) {
+          c[i] = __ldcs(m.indices + j);
+          v[i] = ld_val(vals + j);
+        } else {
+          c[i] = -1;
+          v[i] = 0.f;
+        }
+      }
+    }
+  };
+  auto load_ends = [&](int r) {  // offsets[r + 1 + lane]: end of row r + lane
+    const int k = r + 1 + lane;
+    return k <= rows ? __ldcs(m.offsets + k) : 0x7fffffff;
+  };
+
+  // x at the tile's columns, gathered one tile ahead (a column outside
+  // [0, cols) reads nothing and raises the flag once per range)
+  float xg[kPer];
+  auto gather = [&]() {
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+      const int col = c[i];
+      xg[i] = 0.f;
+      if ((unsigned)col < cols)
+        xg[i] = __ldg(m.x + col);
+      else if (col != -1)
+        bad_col = true;
+    }
+  };
+
+  int ra = rs, lo = ns;  // first row not yet closed; first nonzero of the tile
+  int hi = tile_hi(lo);
+  load_tile(lo, hi);
+  int o = load_ends(ra);
+  gather();
+  Acc<COMP> carry;
+
+  while (lo < ne || ra < re) {
+    // rows [ra, re) ending at or before hi, at most kMaxEnds of them.  The
+    // ends are kept as a list (S.re) and as a 256-bit map of end positions
+    // 1..256 (bit p-1 of W, every lane holding all 8 words): when the ends
+    // are strictly increasing (no empty rows inside the tile, the common
+    // case) a lane reads its 8 end bits and its first row index straight
+    // from the map; otherwise the list is searched.
+    int X = 0;
+    unsigned W[8];
+#pragma unroll
+    for (int w = 0; w < 8; ++w) W[w] = 0u;
+    bool fast = true;
+    int z = 0;  // 1 if the first end is at position 0 (row closed before any nonzero)
+    {
+      int e = o;
+      int prev = -1;
+      for (int base = 0;;) {
+        const bool in = ra + base + lane < re && e <= hi;
+        const unsigned b = __ballot_sync(kFullMask, in);
+        const int cnt = b == kFullMask ? 32 : __ffs(~b) - 1;
+        const int el = min(max(e - lo, 0), hi - lo);
+        if (lane < cnt) S.re[base + lane] = el;
+        int pe = __shfl_up_sync(kFullMask, el, 1);
+        if (lane == 0) pe = prev;
+        fast = __all_sync(kFullMask, fast && (lane >= cnt || el > pe));
+        if (base == 0) z = (cnt > 0 && __shfl_sync(kFullMask, el, 0) == 0) ? 1 : 0;
+        const int bit = (lane < cnt && el >= 1) ? el - 1 : 0x7fffffff;
+#pragma unroll
+        for (int w = 0; w < 8; ++w)
+          W[w] |= __reduce_or_sync(kFullMask, (bit >> 5) == w ? 1u << (bit & 31) : 0u);
+        X = base + cnt;
+        if (cnt < 32 || X >= kMaxEnds) break;
+        prev = __shfl_sync(kFullMask, el, 31);
+        base += 32;
+        const int kx = ra + base + 1 + lane;
+        e = kx <= rows ? __ldg(m.offsets + kx) : 0x7fffffff;
+      }
+    }
+    __syncwarp();
+    if (X >= kMaxEnds) {  // cut the tile at its 256th row end
+      hi = lo + S.re[kMaxEnds - 1];
+      fast = false;
+    }
+    const int Y = hi - lo;
+    if (X == 0 && Y == 0) {  // no progress possible: malformed offsets
+      bad = true;
+      break;
+    }
+
+    // products of this lane's nonzeros 8 lane + i
+    float p[kPer];
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) p[i] = kPer * lane + i < Y ? __fmul_rn(v[i], xg[i]) : 0.f;
+    // the window registers are free: start loading the next tile
+    const int lo2 = hi, hi2 = tile_hi(hi), ra2 = ra + X;
+    if (lo2 < ne) load_tile(lo2, hi2);
+    if (ra2 < re) o = load_ends(ra2);
+
+    // this lane's row ends: end positions in (8 lane, 8 lane + 8] (lane 0:
+    // also position 0), as "close after product i" bits; k = the first row
+    // (tile index) the lane closes, kend = one past its last
+    int k, kend;
+    unsigned mask;
+    Acc<COMP> run, first;
+    if (fast) {
+      const int wl = lane >> 2, sh = kPer * (lane & 3);
+      int pre = 0;
+      unsigned ww = 0u;
+#pragma unroll
+      for (int w = 0; w < 8; ++w) {
+        if (w < wl) pre += __popc(W[w]);
+        if (w == wl) ww = W[w];
+      }
+      const int below = z + pre + __popc(ww & ((1u << sh) - 1u));  // ends at positions <= 8 lane
+      mask = (ww >> sh) & 0xffu;
+      k = lane == 0 ? 0 : below;
+      kend = below + __popc(mask);
+      int kk = below;
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
+        run.add(p[i]);
+        if ((mask >> i) & 1u) {
+          if (kk == k) {
+            first = run;
+          } else {
+            S.yv[kk] = run.s;
+            if (COMP) S.yc[kk] = run.comp();
+          }
+          ++kk;
+          run = Acc<COMP>();
+        }
+      }
+    } else {
+      k = 0;
+      if (lane > 0) {
+        int lo_ = 0, hi_ = X;
+        while (lo_ < hi_) {
+          const int mid = (lo_ + hi_) >> 1;
+          if (S.re[mid] <= kPer * lane) lo_ = mid + 1; else hi_ = mid;
+        }
+        k = lo_;
+      }
+      kend = __shfl_down_sync(kFullMask, k, 1);
+      if (lane == 31) kend = X;
+      // rows of the tile start at 0 (an empty row stays 0); the first end
+      // at each position closes the running sum, further ends there are
+      // empty rows
+      for (int kk = lane; kk < X; kk += 32) {
+        S.yv[kk] = 0.f;
+        if (COMP) S.yc[kk] = 0.f;
+      }
+      mask = 0u;
+      for (int kk = k; kk < kend; ++kk) {
+        const int q = S.re[kk] - kPer * lane;
+        if (q >= 1 && q <= kPer) {
+          if (kk == k || S.re[kk - 1] != S.re[kk]) {
+            mask |= 1u << (q - 1);
+            S.kp[lane][q - 1] = (unsigned char)kk;
+          }
+        } else if (q != 0 || lane != 0) {
+          bad = true;  // an end outside the lane's nonzeros: malformed offsets
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
+        run.add(p[i]);
+        if ((mask >> i) & 1u) {
+          const int kk = S.kp[lane][i];
+          if (kk == k) {
+            first = run;
+          } else {
+            S.yv[kk] = run.s;
+            if (COMP) S.yc[kk] = run.comp();
+          }
+          run = Acc<COMP>();
+        }
+      }
+    }
+    const bool has_end = kend > k;  // the lane closes row ra + k first
+
+    // stitch rows across lanes; lane 0 continues the previous tile's row
+    SegVal<COMP> mine, cin;
+    mine.f = has_end;
+    mine.v = run;
+    cin.f = 0;
+    cin.v = carry;
+    const SegVal<COMP> inc = warp_seg_scan<COMP>(mine);
+    SegVal<COMP> ex;
+    ex.f = __shfl_up_sync(kFullMask, inc.f, 1);
+    ex.v = shfl_up_acc(inc.v, 1);
+    ex = lane == 0 ? cin : seg_combine(cin, ex);
+    if (has_end) {
+      Acc<COMP> val = ex.v;  // earlier parts of the row first
+      val.add(first);
+      if (need_lb && ra + k == rs) {
+        // the range's first row end closes row rs, begun in an earlier
+        // range: finished by the look-back below
+        S.pend = 1;
+        S.pend_s = val.s;
+        S.pend_c = val.comp();
+      }
+      S.yv[k] = val.s;
+      if (COMP) S.yc[k] = val.comp();
+    }
+    __syncwarp();
+    for (int kk = lane; kk < X; kk += 32) {  // coalesced store of the tile's rows
+      const int r = ra + kk;
+      if (need_lb && r == rs) continue;
+      float vv = COMP ? __fadd_rn(S.yv[kk], S.yc[kk]) : S.yv[kk];
+      if (scale) vv *= __ldg(scale + r);
+      m.y[r] = vv;
+    }
+    carry = shfl_idx_acc(seg_combine(cin, inc).v, 31);
+
+    ra = ra2;
+    lo = lo2;
+    hi = hi2;
+    if (lo < ne) gather();  // the next tile's window has arrived by now
+    __syncwarp();  // S.re is rewritten by the next tile
+  }
+  ra_out = ra;
+  return carry;
+}
+
 template <typename VT, bool COMP>
 __global__ void __launch_bounds__(kTPB, 3)
     merge_path_nz_kernel(const Args a) {
@@ -107,10 +389,7 @@ __global__ void __launch_bounds__(kTPB, 3)
   const int lane = threadIdx.x & 31;
   WarpSmem<COMP>& S = smem_all[threadIdx.x >> 5];
   WsHeader* hdr = a.ws.hdr;
-  const VT* vals = reinterpret_cast<const VT*>(a.values);
   const float* __restrict__ scale = a.row_scale;
-  const int rows = (int)a.rows;
-  const unsigned cols = (unsigned)a.cols;
 
   unsigned tk = 0, ep = 0;
   if (lane == 0) {
@@ -137,181 +416,12 @@ __global__ void __launch_bounds__(kTPB, 3)
       if (g == 0 && off_rs != 0) raise_flag(hdr, EL_FLAG_NNZ_MISMATCH, 0);
     }
 
-    // tile [lo, hi): nonzeros up to the next multiple of kTileNz (or ne)
-    auto tile_hi = [&](int l) { return l < ne ? min(ne, (l & ~(kTileNz - 1)) + kTileNz) : l; };
-    int c[kPer];
-    float v[kPer];
-    auto load_tile = [&](int l, int h) {
-      const int j0 = l + kPer * lane;
-      if (a.vec_ok && h - l == kTileNz && (l & 7) == 0) {
-        load8i(a.indices + j0, c);
-        load8(vals + j0, v);
-      } else {
-#pragma unroll
-        for (int i = 0; i < kPer; ++i) {
-          const int j = j0 + i;
-          if (j < h) {
-            c[i] = __ldcs(a.indices + j);
-            v[i] = ld_val(vals + j);
-          } else {
-            c[i] = -1;
-            v[i] = 0.f;
-          }
-        }
-      }
-    };
-    auto load_ends = [&](int r) {  // offsets[r + 1 + lane]: end of row r + lane
-      const int k = r + 1 + lane;
-      return k <= rows ? __ldcs(a.offsets + k) : 0x7fffffff;
-    };
-
-    // x at the tile's columns, gathered one tile ahead (a column outside
-    // [0, cols) reads nothing and raises the flag once per range)
-    float xg[kPer];
-    bool bad_col = false;
-    auto gather = [&]() {
-#pragma unroll
-      for (int i = 0; i < kPer; ++i) {
-        const int col = c[i];
-        xg[i] = 0.f;
-        if ((unsigned)col < cols)
-          xg[i] = __ldg(a.x + col);
-        else if (col != -1)
-          bad_col = true;
-      }
-    };
-
-    int ra = rs, lo = ns;  // first row not yet closed; first nonzero of the tile
-    int hi = tile_hi(lo);
-    load_tile(lo, hi);
-    int o = load_ends(ra);
-    gather();
-    Acc<COMP> carry;
-    bool bad = false;
-
-    while (lo < ne || ra < re) {
-      // rows [ra, re) ending at or before hi, at most kMaxEnds of them
-      int X = 0;
-      {
-        int e = o;
-        for (int base = 0;;) {
-          const bool in = ra + base + lane < re && e <= hi;
-          const unsigned b = __ballot_sync(kFullMask, in);
-          const int cnt = b == kFullMask ? 32 : __ffs(~b) - 1;
-          if (lane < cnt) S.re[base + lane] = min(max(e - lo, 0), hi - lo);
-          X = base + cnt;
-          if (cnt < 32 || X >= kMaxEnds) break;
-          base += 32;
-          const int k = ra + base + 1 + lane;
-          e = k <= rows ? __ldg(a.offsets + k) : 0x7fffffff;
-        }
-      }
-      __syncwarp();
-      if (X >= kMaxEnds) hi = lo + S.re[kMaxEnds - 1];  // cut the tile at its 256th row end
-      const int Y = hi - lo;
-      if (X == 0 && Y == 0) {  // no progress possible: malformed offsets
-        bad = true;
-        break;
-      }
-
-      // products of this lane's nonzeros 8 lane + i
-      float p[kPer];
-#pragma unroll
-      for (int i = 0; i < kPer; ++i) p[i] = kPer * lane + i < Y ? __fmul_rn(v[i], xg[i]) : 0.f;
-      // the window registers are free: start loading the next tile
-      const int lo2 = hi, hi2 = tile_hi(hi), ra2 = ra + X;
-      if (lo2 < ne) load_tile(lo2, hi2);
-      if (ra2 < re) o = load_ends(ra2);
-
-      // this lane's row ends: end positions in (8 lane, 8 lane + 8] (lane 0:
-      // also position 0, rows closed before any nonzero of the tile)
-      int k = 0;
-      if (lane > 0) {
-        int lo_ = 0, hi_ = X;
-        while (lo_ < hi_) {
-          const int mid = (lo_ + hi_) >> 1;
-          if (S.re[mid] <= kPer * lane) lo_ = mid + 1; else hi_ = mid;
-        }
-        k = lo_;
-      }
-      int kend = __shfl_down_sync(kFullMask, k, 1);
-      if (lane == 31) kend = X;
-
-      // rows of the tile start at 0 (an empty row stays 0); the lane's row
-      // ends become "close after product i" bits (the first end at each
-      // position closes the running sum, further ends there are empty rows)
-      for (int kk = lane; kk < X; kk += 32) {
-        S.yv[kk] = 0.f;
-        if (COMP) S.yc[kk] = 0.f;
-      }
-      unsigned mask = 0;
-      for (int kk = k; kk < kend; ++kk) {
-        const int q = S.re[kk] - kPer * lane;
-        if (q >= 1 && q <= kPer) {
-          if (kk == k || S.re[kk - 1] != S.re[kk]) {
-            mask |= 1u << (q - 1);
-            S.kp[lane][q - 1] = (unsigned char)kk;
-          }
-        } else if (q != 0 || lane != 0) {
-          bad = true;  // an end outside the lane's nonzeros: malformed offsets
-        }
-      }
-      __syncwarp();
-      Acc<COMP> run;
-#pragma unroll
-      for (int i = 0; i < kPer; ++i) {
-        run.add(p[i]);
-        if ((mask >> i) & 1u) {
-          const int kk = S.kp[lane][i];
-          S.yv[kk] = run.s;
-          if (COMP) S.yc[kk] = run.comp();
-          run = Acc<COMP>();
-        }
-      }
-      const bool has_end = kend > k;  // the lane closes row ra + k first
-
-      // stitch rows across lanes; lane 0 continues the previous tile's row
-      SegVal<COMP> mine, cin;
-      mine.f = has_end;
-      mine.v = run;
-      cin.f = 0;
-      cin.v = carry;
-      const SegVal<COMP> inc = warp_seg_scan<COMP>(mine);
-      SegVal<COMP> ex;
-      ex.f = __shfl_up_sync(kFullMask, inc.f, 1);
-      ex.v = shfl_up_acc(inc.v, 1);
-      ex = lane == 0 ? cin : seg_combine(cin, ex);
-      if (has_end) {
-        Acc<COMP> val = ex.v;  // earlier parts of the row first
-        Acc<COMP> mine_part;
-        mine_part.set(S.yv[k], COMP ? S.yc[k] : 0.f);
-        val.add(mine_part);
-        if (need_lb && ra + k == rs) {
-          // the range's first row end closes row rs, begun in an earlier
-          // range: finished by the look-back below
-          S.pend = 1;
-          S.pend_s = val.s;
-          S.pend_c = val.comp();
-        }
-        S.yv[k] = val.s;
-        if (COMP) S.yc[k] = val.comp();
-      }
-      __syncwarp();
-      for (int kk = lane; kk < X; kk += 32) {  // coalesced store of the tile's rows
-        const int r = ra + kk;
-        if (need_lb && r == rs) continue;
-        float vv = COMP ? __fadd_rn(S.yv[kk], S.yc[kk]) : S.yv[kk];
-        if (scale) vv *= __ldg(scale + r);
-        a.y[r] = vv;
-      }
-      carry = shfl_idx_acc(seg_combine(cin, inc).v, 31);
-
-      ra = ra2;
-      lo = lo2;
-      hi = hi2;
-      if (lo < ne) gather();  // the next tile's window has arrived by now
-      __syncwarp();  // S.re is rewritten by the next tile
-    }
+    const Src m{a.offsets, a.indices,  a.values, a.row_scale, a.x,
+                a.y,       (int)a.rows, (unsigned)a.cols, a.vec_ok, a.ph};
+    bool bad = false, bad_col = false;
+    int ra = rs;
+    const Acc<COMP> carry =
+        walk_rows<VT, COMP>(m, S, lane, rs, re, ns, ne, need_lb, bad, bad_col, ra);
     if (__any_sync(kFullMask, bad_col) && lane == 0)
       raise_flag(hdr, EL_FLAG_INDEX_RANGE, (unsigned)ra);
     if (__any_sync(kFullMask, bad) && lane == 0) raise_flag(hdr, EL_FLAG_OFFSETS, (unsigned)ra);
@@ -414,7 +524,7 @@ el_status launch(const SpmvCall& c) {
   a.y = c.y;
   a.range_items = upr * kTileNz;
   a.num_ranges = (units + upr - 1) / upr;
-  a.vec_ok = ((uintptr_t)c.A.indices % 16) == 0 && ((uintptr_t)c.A.values % 16) == 0;
+  tile_phase(c.A.indices, c.A.values, (int)sizeof(VT), &a.vec_ok, &a.ph);
   a.test_hooks = c.o.test_hooks;
   a.wait_ns = c.wait_ns;
   a.ws = c.ws;

@@ -63,7 +63,7 @@ el_status launch_static(const el_csr& A, const float* x, float* y, int ranges, v
   a.y = y;
   a.range_items = upr * kTileNz;
   a.num_ranges = (units + upr - 1) / upr;
-  a.vec_ok = ((uintptr_t)A.indices % 16) == 0 && ((uintptr_t)A.values % 16) == 0;
+  tile_phase(A.indices, A.values, (int)sizeof(VT), &a.vec_ok, &a.ph);
   a.test_hooks = 0;
   a.wait_ns = 2000000000ull;
   a.ws.hdr = reinterpret_cast<WsHeader*>(scratch);

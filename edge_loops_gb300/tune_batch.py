@@ -1,7 +1,8 @@
 """Autotuner for the batched SpMV plan: measures, per (rows, mean row length,
-row-length variation) bucket, which threads-per-row and work-item size run a
-group of matrices of that bucket fastest, and writes the table
-el_batch_plan_create reads (JSON, loaded by api.load_tuning_table).
+row-length variation) bucket, which kernel mode (1..32 lanes per row or the
+nonzero-tiled walk) and work-item size run a group of matrices of that
+bucket fastest, and writes the table el_batch_plan_create reads (JSON,
+loaded by api.load_tuning_table).
 
     python -m edge_loops_gb300.tune_batch [--dtype bf16] [--out PATH]
 
@@ -25,8 +26,8 @@ import torch
 from . import _lib as L
 from . import api, synth
 
-TPRS = (1, 2, 4, 8, 16, 32)
-CHUNKS = (10, 12, 14)
+TPRS = (1, 2, 4, 8, 16, 32, L.EL_BATCH_NZ_WALK)  # lanes per row, or the nonzero-tiled walk
+CHUNKS = (8, 10, 12, 14)  # log2(rows + nonzeros) per work item
 ROW_BUCKETS = (6, 8, 10, 12, 14, 16)
 LEN_BUCKETS = (1, 2, 3, 4, 5, 6, 7, 8)
 SIGMAS = (0.1, 0.5, 1.0, 1.5)  # aims at variation buckets 0..3

@@ -213,12 +213,14 @@ el_status el_work_oriented_partition(const int32_t* offsets, int64_t rows,
  * Thousands of independent CSR matrices, each with its own x and y, run in
  * ONE persistent launch that the plan captures in a CUDA graph.  A plan
  * computes row-length statistics of every matrix on the device, picks per
- * matrix a threads-per-row and a chunk size from a tuning table indexed by
- * (rows, mean row length, row-length variation) buckets, splits every
- * matrix into row chunks of about that many nonzeros and stores the work
- * list on the device.  Matrices with a row longer than
- * EL_BATCH_MAX_ROW_NNZ run as their own merge-path launches inside the same
- * graph.  All matrices of a plan share one value dtype. */
+ * matrix a kernel mode (the nonzero-tiled warp walk of the merge-path
+ * kernel, or 1..32 lanes per row) and a work-item size from a tuning table
+ * indexed by (rows, mean row length, row-length variation) buckets, cuts
+ * every matrix into work items of whole rows at merge-path diagonals (about
+ * 2^chunk rows + nonzeros each) and keeps the work list on the device.
+ * Matrices with a row longer than EL_BATCH_MAX_ROW_NNZ run as their own
+ * merge-path launches inside the same graph.  All matrices of a plan share
+ * one value dtype. */
 typedef struct el_batch_item {
   el_csr A;
   const float* x;
@@ -231,15 +233,18 @@ typedef struct el_batch_item {
 #define EL_BATCH_TABLE_SIZE \
   (EL_BATCH_ROW_BUCKETS * EL_BATCH_LEN_BUCKETS * EL_BATCH_CV_BUCKETS)
 /* table index = (row_bucket * EL_BATCH_LEN_BUCKETS + len_bucket) *
- * EL_BATCH_CV_BUCKETS + cv_bucket; entry = threads_per_row (1..32) |
- * log2(nonzeros per work item) << 8, or 0 for the built-in rule. */
+ * EL_BATCH_CV_BUCKETS + cv_bucket; entry = threads_per_row (1..32, or
+ * EL_BATCH_NZ_WALK) | log2(rows + nonzeros per work item) << 8, or 0 for
+ * the built-in rule (nonzero-tiled walk, 2^12). */
+#define EL_BATCH_NZ_WALK 64
 #define EL_BATCH_MAX_ROW_NNZ 16384
 
 typedef struct el_batch_opts {
   const int32_t* table;          /* EL_BATCH_TABLE_SIZE entries or NULL */
   int32_t use_graph;             /* 1: capture in a CUDA graph (default 1 via
                                     el_batch_opts_default) */
-  int32_t force_threads_per_row; /* > 0: this for every matrix (tuning) */
+  int32_t force_threads_per_row; /* > 0: this (1..32 or EL_BATCH_NZ_WALK) for
+                                    every matrix (tuning) */
   int32_t force_chunk_log2;      /* > 0: this for every matrix (tuning) */
   int32_t max_ctas;              /* cap on the persistent grid (0 = resident) */
   int32_t reserved[8];
@@ -255,8 +260,9 @@ el_status el_batch_plan_create(const el_batch_item* items, int32_t count,
                                el_batch_plan** out);
 /* One y = A x for every matrix of the plan, asynchronous on `stream`. */
 el_status el_batch_plan_execute(el_batch_plan* plan, el_stream_t stream);
-/* Work items, matrices per threads-per-row value (tpr_counts[6] for
- * 1,2,4,8,16,32) and matrices run as separate merge-path launches. */
+/* Work items, matrices per kernel mode (tpr_counts[7]: 1,2,4,8,16,32 lanes
+ * per row, nonzero-tiled walk) and matrices run as separate merge-path
+ * launches. */
 el_status el_batch_plan_info(const el_batch_plan* plan, int64_t* work_items,
                              int32_t* tpr_counts, int32_t* heavy);
 /* Synchronises `stream` and returns (and optionally clears) the EL_FLAG_*

@@ -35,7 +35,7 @@ def check(oracle_mod, items, scale_of=None, vals_of=None):
 
 
 @pytest.mark.parametrize("use_graph", [True, False])
-@pytest.mark.parametrize("tpr", [0, 1, 4, 32])
+@pytest.mark.parametrize("tpr", [0, 1, 4, 32, 64])
 def test_batched_f32(cuda, oracle_mod, use_graph, tpr):
     from edge_loops_gb300 import api
     items, y = make(cuda)
@@ -43,6 +43,8 @@ def test_batched_f32(cuda, oracle_mod, use_graph, tpr):
     plan = api.BatchPlan(items, use_graph=use_graph, force_threads_per_row=tpr)
     info = plan.info()
     assert info["heavy_matrices"] == 0 and info["work_items"] > 0
+    if tpr == 64:
+        assert info["matrices_nz_walk"] == len(items)
     plan.execute()
     assert plan.errors() == 0
     check(oracle_mod, items)
@@ -93,14 +95,51 @@ def test_heavy_empty_and_tiny_matrices(cuda, oracle_mod):
     check(oracle_mod, items)
 
 
-def test_table_drives_configuration(cuda, oracle_mod):
+@pytest.mark.parametrize("entry", [16 | (11 << 8), 64 | (7 << 8), 2 | (14 << 8)])
+def test_table_drives_configuration(cuda, oracle_mod, entry):
     from edge_loops_gb300 import api, _lib
     items, y = make(cuda, count=32)
-    table = np.full(_lib.EL_BATCH_TABLE_SIZE, 16 | (11 << 8), dtype=np.int32)
+    table = np.full(_lib.EL_BATCH_TABLE_SIZE, entry, dtype=np.int32)
     plan = api.BatchPlan(items, table=table)
-    assert plan.info()["matrices_by_threads_per_row"][16] == 32
+    info = plan.info()
+    if entry & 0xff == 64:
+        assert info["matrices_nz_walk"] == 32
+    else:
+        assert info["matrices_by_threads_per_row"][entry & 0xff] == 32
     plan.execute()
+    assert plan.errors() == 0
     check(oracle_mod, items)
+
+
+def test_nz_walk_unaligned_and_ragged(cuda, oracle_mod):
+    """Matrices whose indices/values start at every phase modulo 8 elements
+    (the walk's 128-bit loads need a common phase; mismatched phases fall
+    back to scalar loads), rows from empty to thousands of nonzeros, and
+    items of 2^6 rows + nonzeros (many items per matrix)."""
+    from edge_loops_gb300 import api
+    from conftest import random_csr
+    rng = np.random.default_rng(11)
+    items = []
+    keep = []
+    for m in range(24):
+        off, idx, vals, x = random_csr(rng, rows=int(rng.integers(1, 700)), cols=900,
+                                       max_len=int(rng.integers(1, 80)), empty_frac=0.2)
+        nnz = len(idx)
+        si, sv = m % 8, (m * 3) % 8 if m % 3 else m % 8
+        ib = torch.zeros(nnz + 16, dtype=torch.int32, device=cuda)
+        vb = torch.zeros(nnz + 16, dtype=torch.float32, device=cuda)
+        ib[si: si + nnz] = torch.as_tensor(idx, device=cuda)
+        vb[sv: sv + nnz] = torch.as_tensor(vals, device=cuda)
+        keep += [ib, vb]
+        A = api.CSR(torch.as_tensor(off, device=cuda), ib[si: si + nnz], vb[sv: sv + nnz],
+                    len(off) - 1, 900)
+        items.append((A, torch.as_tensor(x, device=cuda),
+                      torch.full((A.rows,), float("nan"), device=cuda)))
+    for chunk in (6, 12):
+        plan = api.BatchPlan(items, force_threads_per_row=64, force_chunk_log2=chunk)
+        plan.execute()
+        assert plan.errors() == 0
+        check(oracle_mod, items)
 
 
 def test_malformed_matrix_rejected(cuda):
