@@ -130,8 +130,9 @@ __device__ __forceinline__ void rows_nz(const Desc& d, int r0, int r1, int lane,
                                         mpn::WarpSmem<false>& S, bool& bad, bool& bad_col) {
   const int ns = min(max(__ldg(d.offsets + r0), 0), d.nnz);
   const int ne = min(max(__ldg(d.offsets + r1), ns), d.nnz);
-  const mpn::Src m{d.offsets, d.indices, d.values, d.row_scale, d.x, d.y,
-                   d.rows,    (unsigned)d.cols, d.ph >= 0 ? 1 : 0, d.ph >= 0 ? d.ph : 0};
+  const mpn::Src m{d.offsets, d.indices,        d.values, d.row_scale,       d.x,
+                   d.y,       d.rows,           (unsigned)d.cols, d.nnz, d.ph >= 0 ? 1 : 0,
+                   d.ph >= 0 ? d.ph : 0};
   int ra = r0;
   (void)mpn::walk_rows<VT, false>(m, S, lane, r0, r1, ns, ne, false, bad, bad_col, ra);
 }

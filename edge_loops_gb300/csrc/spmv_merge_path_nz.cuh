@@ -53,11 +53,12 @@ struct Args {
 };
 
 template <bool COMP>
-struct WarpSmem {
+struct __align__(16) WarpSmem {
   int re[kMaxEnds];            // end position (tile-local nonzero index) of each row end
-  float yv[kMaxEnds];          // the tile's row sums, staged for one coalesced store
-  float yc[COMP ? kMaxEnds : 1];
+  float yv[kMaxEnds];          // the tile's row sums (or, whole tiles, sums by end position)
+  float yc[COMP ? kMaxEnds : 4];
   unsigned char kp[32][kPer];  // row end closed after lane l's product i (tile-local)
+  unsigned bits[8];            // whole tiles: bit p-1 = a row ends after nonzero p-1
   int pend;
   float pend_s, pend_c;
 };
@@ -111,6 +112,7 @@ struct Src {
   float* y;
   int rows;
   unsigned cols;
+  int nnz;
   int vec_ok;  // 128-bit loads allowed at tile starts
   int ph;      // tiles start where (nonzero index + ph) is a multiple of kTileNz
 };
@@ -146,8 +148,8 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
   // tile [lo, hi): nonzeros up to the next multiple of kTileNz (or ne)
   auto tile_hi = [&](int l) -> int {
     if (l >= ne) return l;
-    const long long t = (((long long)l + m.ph) & ~(long long)(kTileNz - 1)) + kTileNz - m.ph;
-    return t < ne ? (int)t : ne;
+    const unsigned t = (((unsigned)l + m.ph) & ~(unsigned)(kTileNz - 1)) + kTileNz - m.ph;
+    return t < (unsigned)ne ? (int)t : ne;
   };
   int c[kPer];
   float v[kPer];
@@ -190,6 +192,7 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
     }
   };
 
+  if (lane < 8) S.bits[lane] = 0u;
   int ra = rs, lo = ns;  // first row not yet closed; first nonzero of the tile
   int hi = tile_hi(lo);
   load_tile(lo, hi);
@@ -198,48 +201,36 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
   Acc<COMP> carry;
 
   while (lo < ne || ra < re) {
-    // rows [ra, re) ending at or before hi, at most kMaxEnds of them.  The
-    // ends are kept as a list (S.re) and as a 256-bit map of end positions
-    // 1..256 (bit p-1 of W, every lane holding all 8 words): when the ends
-    // are strictly increasing (no empty rows inside the tile, the common
-    // case) a lane reads its 8 end bits and its first row index straight
-    // from the map; otherwise the list is searched.
-    int X = 0;
-    unsigned W[8];
-#pragma unroll
-    for (int w = 0; w < 8; ++w) W[w] = 0u;
-    bool fast = true;
-    int z = 0;  // 1 if the first end is at position 0 (row closed before any nonzero)
+    // rows [ra, re) ending at or before hi, at most kMaxEnds of them: their
+    // end positions in the tile (S.re; the first 32 also in el0)
+    int X = 0, el0 = 0;
+    bool rising = true;  // end positions strictly increasing (no empty rows)
     {
       int e = o;
       int prev = -1;
       for (int base = 0;;) {
-        const bool in = ra + base + lane < re && e <= hi;
+        const bool in = (unsigned)(ra + base + lane) < (unsigned)re && e <= hi;
         const unsigned b = __ballot_sync(kFullMask, in);
         const int cnt = b == kFullMask ? 32 : __ffs(~b) - 1;
-        const int el = min(max(e - lo, 0), hi - lo);
-        if (lane < cnt) S.re[base + lane] = el;
+        const int el = (e <= hi ? max(e, lo) : hi) - lo;
         int pe = __shfl_up_sync(kFullMask, el, 1);
         if (lane == 0) pe = prev;
-        fast = __all_sync(kFullMask, fast && (lane >= cnt || el > pe));
-        if (base == 0) z = (cnt > 0 && __shfl_sync(kFullMask, el, 0) == 0) ? 1 : 0;
-        const int bit = (lane < cnt && el >= 1) ? el - 1 : 0x7fffffff;
-#pragma unroll
-        for (int w = 0; w < 8; ++w)
-          W[w] |= __reduce_or_sync(kFullMask, (bit >> 5) == w ? 1u << (bit & 31) : 0u);
+        if (lane < cnt) {
+          S.re[base + lane] = el;
+          rising = rising && el > pe;
+        }
+        if (base == 0) el0 = el;
         X = base + cnt;
         if (cnt < 32 || X >= kMaxEnds) break;
         prev = __shfl_sync(kFullMask, el, 31);
         base += 32;
-        const int kx = ra + base + 1 + lane;
-        e = kx <= rows ? __ldg(m.offsets + kx) : 0x7fffffff;
+        const int k = ra + base + 1 + lane;
+        e = k <= rows ? __ldg(m.offsets + k) : 0x7fffffff;
       }
     }
+    const bool fast = __all_sync(kFullMask, rising) && X < kMaxEnds && hi - lo == kTileNz;
     __syncwarp();
-    if (X >= kMaxEnds) {  // cut the tile at its 256th row end
-      hi = lo + S.re[kMaxEnds - 1];
-      fast = false;
-    }
+    if (X >= kMaxEnds) hi = lo + S.re[kMaxEnds - 1];  // cut the tile at its 256th row end
     const int Y = hi - lo;
     if (X == 0 && Y == 0) {  // no progress possible: malformed offsets
       bad = true;
@@ -248,49 +239,102 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
 
     // products of this lane's nonzeros 8 lane + i
     float p[kPer];
+    if (fast) {
 #pragma unroll
-    for (int i = 0; i < kPer; ++i) p[i] = kPer * lane + i < Y ? __fmul_rn(v[i], xg[i]) : 0.f;
+      for (int i = 0; i < kPer; ++i) p[i] = __fmul_rn(v[i], xg[i]);
+    } else {
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) p[i] = kPer * lane + i < Y ? __fmul_rn(v[i], xg[i]) : 0.f;
+    }
     // the window registers are free: start loading the next tile
     const int lo2 = hi, hi2 = tile_hi(hi), ra2 = ra + X;
     if (lo2 < ne) load_tile(lo2, hi2);
     if (ra2 < re) o = load_ends(ra2);
 
-    // this lane's row ends: end positions in (8 lane, 8 lane + 8] (lane 0:
-    // also position 0), as "close after product i" bits; k = the first row
-    // (tile index) the lane closes, kend = one past its last
-    int k, kend;
-    unsigned mask;
-    Acc<COMP> run, first;
     if (fast) {
-      const int wl = lane >> 2, sh = kPer * (lane & 3);
-      int pre = 0;
-      unsigned ww = 0u;
-#pragma unroll
-      for (int w = 0; w < 8; ++w) {
-        if (w < wl) pre += __popc(W[w]);
-        if (w == wl) ww = W[w];
+      // Whole tile, strictly increasing row ends.  A lane's close bits come
+      // from a map of the end positions (bit p-1 of S.bits = a row ends
+      // after nonzero p-1); the lane's running sums are staged by position
+      // (S.yv[q] = its products since its previous close, up to nonzero q),
+      // its tail is stitched by a segmented scan whose segment starts come
+      // from one ballot, and row r's sum is read back at its end position.
+      for (int kk = lane; kk < X; kk += 32) {
+        const int P = kk < 32 ? el0 : S.re[kk];
+        if (P > 0) atomicOr(&S.bits[(P - 1) >> 5], 1u << ((P - 1) & 31));
       }
-      const int below = z + pre + __popc(ww & ((1u << sh) - 1u));  // ends at positions <= 8 lane
-      mask = (ww >> sh) & 0xffu;
-      k = lane == 0 ? 0 : below;
-      kend = below + __popc(mask);
-      int kk = below;
+      __syncwarp();
+      const unsigned mask = (S.bits[lane >> 2] >> (kPer * (lane & 3))) & 0xffu;
+      Acc<COMP> run;
+      float ss[kPer], sc[kPer];
 #pragma unroll
       for (int i = 0; i < kPer; ++i) {
         run.add(p[i]);
-        if ((mask >> i) & 1u) {
-          if (kk == k) {
-            first = run;
-          } else {
-            S.yv[kk] = run.s;
-            if (COMP) S.yc[kk] = run.comp();
-          }
-          ++kk;
-          run = Acc<COMP>();
+        ss[i] = run.s;
+        sc[i] = run.comp();
+        if ((mask >> i) & 1u) run = Acc<COMP>();
+      }
+      reinterpret_cast<float4*>(&S.yv[kPer * lane])[0] = make_float4(ss[0], ss[1], ss[2], ss[3]);
+      reinterpret_cast<float4*>(&S.yv[kPer * lane])[1] = make_float4(ss[4], ss[5], ss[6], ss[7]);
+      if (COMP) {
+        reinterpret_cast<float4*>(&S.yc[kPer * lane])[0] = make_float4(sc[0], sc[1], sc[2], sc[3]);
+        reinterpret_cast<float4*>(&S.yc[kPer * lane])[1] = make_float4(sc[4], sc[5], sc[6], sc[7]);
+      }
+      // a row closed at position 0 (before the tile's first nonzero) takes
+      // the carry; otherwise the carry runs into the first lanes
+      const bool z = X > 0 && __shfl_sync(kFullMask, el0, 0) == 0;
+      const Acc<COMP> cin = z ? Acc<COMP>() : carry;
+      const unsigned heads = __ballot_sync(kFullMask, mask != 0u);
+      const unsigned upto = heads & (lane == 31 ? 0xffffffffu : (2u << lane) - 1u);
+      const int dist = upto ? lane - (31 - __clz(upto)) : lane;  // lanes since my segment began
+      Acc<COMP> inc = run;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        Acc<COMP> t = shfl_up_acc(inc, d);
+        if (d <= dist) {
+          t.add(inc);  // earlier lanes first
+          inc = t;
         }
       }
+      if (!upto) {
+        Acc<COMP> t = cin;
+        t.add(inc);
+        inc = t;
+      }
+      Acc<COMP> ex = shfl_up_acc(inc, 1);
+      if (lane == 0) ex = cin;
+      const Acc<COMP> cout = shfl_idx_acc(inc, 31);
+      if (mask) {  // the lane's first close: earlier parts of the row first
+        const int f = kPer * lane + __ffs(mask) - 1;
+        Acc<COMP> mine;
+        mine.set(S.yv[f], COMP ? S.yc[f] : 0.f);
+        ex.add(mine);
+        S.yv[f] = ex.s;
+        if (COMP) S.yc[f] = ex.comp();
+      }
+      __syncwarp();
+      if (lane < 8) S.bits[lane] = 0u;  // every lane has read its mask
+      for (int kk = lane; kk < X; kk += 32) {  // coalesced store of the tile's rows
+        const int P = kk < 32 ? el0 : S.re[kk];
+        Acc<COMP> val = carry;
+        if (P > 0) val.set(S.yv[P - 1], COMP ? S.yc[P - 1] : 0.f);
+        const int r = ra + kk;
+        if (need_lb && r == rs) {
+          // the range's first row end closes row rs, begun in an earlier
+          // range: finished by the look-back
+          S.pend = 1;
+          S.pend_s = val.s;
+          S.pend_c = val.comp();
+          continue;
+        }
+        float vv = val.value();
+        if (scale) vv *= __ldg(scale + r);
+        m.y[r] = vv;
+      }
+      carry = cout;
     } else {
-      k = 0;
+      // this lane's row ends: end positions in (8 lane, 8 lane + 8] (lane 0:
+      // also position 0, rows closed before any nonzero of the tile)
+      int k = 0;
       if (lane > 0) {
         int lo_ = 0, hi_ = X;
         while (lo_ < hi_) {
@@ -299,16 +343,17 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
         }
         k = lo_;
       }
-      kend = __shfl_down_sync(kFullMask, k, 1);
+      int kend = __shfl_down_sync(kFullMask, k, 1);
       if (lane == 31) kend = X;
-      // rows of the tile start at 0 (an empty row stays 0); the first end
-      // at each position closes the running sum, further ends there are
-      // empty rows
+
+      // rows of the tile start at 0 (an empty row stays 0); the lane's row
+      // ends become "close after product i" bits (the first end at each
+      // position closes the running sum, further ends there are empty rows)
       for (int kk = lane; kk < X; kk += 32) {
         S.yv[kk] = 0.f;
         if (COMP) S.yc[kk] = 0.f;
       }
-      mask = 0u;
+      unsigned mask = 0;
       for (int kk = k; kk < kend; ++kk) {
         const int q = S.re[kk] - kPer * lane;
         if (q >= 1 && q <= kPer) {
@@ -321,73 +366,85 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
         }
       }
       __syncwarp();
+      Acc<COMP> run;
 #pragma unroll
       for (int i = 0; i < kPer; ++i) {
         run.add(p[i]);
         if ((mask >> i) & 1u) {
           const int kk = S.kp[lane][i];
-          if (kk == k) {
-            first = run;
-          } else {
-            S.yv[kk] = run.s;
-            if (COMP) S.yc[kk] = run.comp();
-          }
+          S.yv[kk] = run.s;
+          if (COMP) S.yc[kk] = run.comp();
           run = Acc<COMP>();
         }
       }
-    }
-    const bool has_end = kend > k;  // the lane closes row ra + k first
+      const bool has_end = kend > k;  // the lane closes row ra + k first
 
-    // stitch rows across lanes; lane 0 continues the previous tile's row
-    SegVal<COMP> mine, cin;
-    mine.f = has_end;
-    mine.v = run;
-    cin.f = 0;
-    cin.v = carry;
-    const SegVal<COMP> inc = warp_seg_scan<COMP>(mine);
-    SegVal<COMP> ex;
-    ex.f = __shfl_up_sync(kFullMask, inc.f, 1);
-    ex.v = shfl_up_acc(inc.v, 1);
-    ex = lane == 0 ? cin : seg_combine(cin, ex);
-    if (has_end) {
-      Acc<COMP> val = ex.v;  // earlier parts of the row first
-      val.add(first);
-      if (need_lb && ra + k == rs) {
-        // the range's first row end closes row rs, begun in an earlier
-        // range: finished by the look-back below
-        S.pend = 1;
-        S.pend_s = val.s;
-        S.pend_c = val.comp();
+      // stitch rows across lanes; lane 0 continues the previous tile's row
+      SegVal<COMP> mine, cin;
+      mine.f = has_end;
+      mine.v = run;
+      cin.f = 0;
+      cin.v = carry;
+      const SegVal<COMP> inc = warp_seg_scan<COMP>(mine);
+      SegVal<COMP> ex;
+      ex.f = __shfl_up_sync(kFullMask, inc.f, 1);
+      ex.v = shfl_up_acc(inc.v, 1);
+      ex = lane == 0 ? cin : seg_combine(cin, ex);
+      if (has_end) {
+        Acc<COMP> val = ex.v;  // earlier parts of the row first
+        Acc<COMP> mine_part;
+        mine_part.set(S.yv[k], COMP ? S.yc[k] : 0.f);
+        val.add(mine_part);
+        if (need_lb && ra + k == rs) {
+          // the range's first row end closes row rs, begun in an earlier
+          // range: finished by the look-back below
+          S.pend = 1;
+          S.pend_s = val.s;
+          S.pend_c = val.comp();
+        }
+        S.yv[k] = val.s;
+        if (COMP) S.yc[k] = val.comp();
       }
-      S.yv[k] = val.s;
-      if (COMP) S.yc[k] = val.comp();
+      __syncwarp();
+      for (int kk = lane; kk < X; kk += 32) {  // coalesced store of the tile's rows
+        const int r = ra + kk;
+        if (need_lb && r == rs) continue;
+        float vv = COMP ? __fadd_rn(S.yv[kk], S.yc[kk]) : S.yv[kk];
+        if (scale) vv *= __ldg(scale + r);
+        m.y[r] = vv;
+      }
+      carry = shfl_idx_acc(seg_combine(cin, inc).v, 31);
     }
-    __syncwarp();
-    for (int kk = lane; kk < X; kk += 32) {  // coalesced store of the tile's rows
-      const int r = ra + kk;
-      if (need_lb && r == rs) continue;
-      float vv = COMP ? __fadd_rn(S.yv[kk], S.yc[kk]) : S.yv[kk];
-      if (scale) vv *= __ldg(scale + r);
-      m.y[r] = vv;
-    }
-    carry = shfl_idx_acc(seg_combine(cin, inc).v, 31);
 
     ra = ra2;
     lo = lo2;
     hi = hi2;
     if (lo < ne) gather();  // the next tile's window has arrived by now
-    __syncwarp();  // S.re is rewritten by the next tile
+    __syncwarp();  // S.re and S.yv are rewritten by the next tile
   }
   ra_out = ra;
   return carry;
 }
 
-template <typename VT, bool COMP>
-__global__ void __launch_bounds__(kTPB, 3)
-    merge_path_nz_kernel(const Args a) {
-  __shared__ WarpSmem<COMP> smem_all[kWarps];
+// The walk of this file as a policy of run_range.
+struct NzWalk {
+  template <typename VT, bool COMP, typename SmemT>
+  static __device__ __forceinline__ Acc<COMP> walk(const Src& m, SmemT& S, int lane, int rs,
+                                                   int re, int ns, int ne, bool need_lb,
+                                                   bool& bad, bool& bad_col, int& ra) {
+    return walk_rows<VT, COMP>(m, S, lane, rs, re, ns, ne, need_lb, bad, bad_col, ra);
+  }
+};
+
+// One warp's merge range, shared by the merge-path kernels: takes a range
+// id from the ticket, finds its split points, walks it with `Walk`
+// (rows ending inside are written), publishes the partial of the row left
+// open at its end, and finishes the row it began with (begun in earlier
+// ranges) by the look-back.  `SmemT` is the walk's per-warp shared memory
+// (with the pend fields).  `warps_per_cta` warps share a CTA.
+template <typename VT, bool COMP, typename Walk, typename SmemT>
+__device__ __forceinline__ void run_range(const Args& a, SmemT& S, const int warps_per_cta) {
   const int lane = threadIdx.x & 31;
-  WarpSmem<COMP>& S = smem_all[threadIdx.x >> 5];
   WsHeader* hdr = a.ws.hdr;
   const float* __restrict__ scale = a.row_scale;
 
@@ -416,12 +473,12 @@ __global__ void __launch_bounds__(kTPB, 3)
       if (g == 0 && off_rs != 0) raise_flag(hdr, EL_FLAG_NNZ_MISMATCH, 0);
     }
 
-    const Src m{a.offsets, a.indices,  a.values, a.row_scale, a.x,
-                a.y,       (int)a.rows, (unsigned)a.cols, a.vec_ok, a.ph};
+    const Src m{a.offsets, a.indices,        a.values,      a.row_scale, a.x,  a.y,
+                (int)a.rows, (unsigned)a.cols, (int)a.nnz, a.vec_ok,    a.ph};
     bool bad = false, bad_col = false;
     int ra = rs;
     const Acc<COMP> carry =
-        walk_rows<VT, COMP>(m, S, lane, rs, re, ns, ne, need_lb, bad, bad_col, ra);
+        Walk::template walk<VT, COMP>(m, S, lane, rs, re, ns, ne, need_lb, bad, bad_col, ra);
     if (__any_sync(kFullMask, bad_col) && lane == 0)
       raise_flag(hdr, EL_FLAG_INDEX_RANGE, (unsigned)ra);
     if (__any_sync(kFullMask, bad) && lane == 0) raise_flag(hdr, EL_FLAG_OFFSETS, (unsigned)ra);
@@ -489,10 +546,17 @@ __global__ void __launch_bounds__(kTPB, 3)
   // the last warp to finish hands the workspace back for the next launch
   if (lane == 0) {
     __threadfence();
-    const unsigned total_warps = gridDim.x * kWarps;
+    const unsigned total_warps = gridDim.x * (unsigned)warps_per_cta;
     const unsigned prev = atomicAdd(&hdr->done, 1u);
     if (prev == total_warps - 1) finish_launch(hdr, epoch);
   }
+}
+
+template <typename VT, bool COMP>
+__global__ void __launch_bounds__(kTPB, 3)
+    merge_path_nz_kernel(const Args a) {
+  __shared__ WarpSmem<COMP> smem_all[kWarps];
+  run_range<VT, COMP, NzWalk>(a, smem_all[threadIdx.x >> 5], kWarps);
 }
 
 template <typename VT, bool COMP>

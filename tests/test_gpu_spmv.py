@@ -121,6 +121,33 @@ def test_edge_cases(cuda, oracle_mod, sched, opts):
         check_against_oracle(oracle_mod, off, idx, vals, x, y)
 
 
+@pytest.mark.parametrize("opts", [{}, {"compensated": True}, {"variant": 2}, {"max_ctas": 2}])
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+def test_merge_path_unaligned_arrays(cuda, oracle_mod, opts, dtype):
+    """indices and values starting at every phase modulo 8 elements, equal
+    (vector copies, cells shifted to the common phase) or not (element-wise
+    copies), and arrays that end inside a 16-byte chunk."""
+    from edge_loops_gb300 import api
+    rng = np.random.default_rng(21)
+    off, idx, vals, x = random_csr(rng, rows=3000, cols=5000, max_len=40, empty_frac=0.1,
+                                   long_rows=[(7, 3000)])
+    nnz = len(idx)
+    xt = torch.as_tensor(x, device=cuda)
+    offt = torch.as_tensor(off, device=cuda)
+    vq = torch.as_tensor(vals).to(dtype)
+    v64 = vq.float().numpy()
+    for si, sv in [(0, 0), (1, 1), (3, 3), (5, 5), (7, 7), (1, 0), (2, 5), (6, 3)]:
+        ib = torch.zeros(nnz + 8, dtype=torch.int32, device=cuda)
+        vb = torch.zeros(nnz + 8, dtype=dtype, device=cuda)
+        ib[si: si + nnz] = torch.as_tensor(idx, device=cuda)
+        vb[sv: sv + nnz] = vq.to(cuda)
+        A = api.CSR(offt, ib[si: si + nnz], vb[sv: sv + nnz], len(off) - 1, len(x))
+        y = torch.full((A.rows,), float("nan"), device=cuda)
+        api.spmv(A, xt, y, schedule="merge_path_flat", **opts)
+        assert api.workspace_errors() == 0
+        check_against_oracle(oracle_mod, off, idx, v64, x, y.cpu().numpy())
+
+
 def test_long_rows_across_many_ctas(cuda, oracle_mod):
     """Rows much longer than a CTA's range: the cross-range carry chain."""
     rng = np.random.default_rng(13)
