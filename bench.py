@@ -167,7 +167,7 @@ def run_ours(args, rank, world):
     A = api.CSR(W["off"], W["idx"], W["vals"], W["rows"], W["cols"])
     if args.value_dtype != "f32":
         tdt = torch.bfloat16 if args.value_dtype == "bf16" else torch.float16
-        A = A.quantized(tdt, per_row_scale=True)
+        A = A.quantized(tdt, per_row_scale=not args.no_row_scale)
     x = W["x"]
     y = torch.empty(A.rows, dtype=torch.float32, device=dev)
     nbytes = synth.algorithmic_bytes(A.rows, A.cols, A.nnz, value_bytes(args.value_dtype),
@@ -286,7 +286,7 @@ def verify(args, A, x, y, W):
         scale = None
     else:
         vals = A.values.float().cpu().numpy()
-        scale = A.row_scale.cpu().numpy()
+        scale = A.row_scale.cpu().numpy() if A.row_scale is not None else None
     y64, yabs = oracle.spmv_f64(off, idx, vals, xx, row_scale=scale)
     u = 2.0 ** -24
     n = np.diff(off.astype(np.int64)) + 2
@@ -632,6 +632,8 @@ def main():
     ap.add_argument("--variant", type=int, default=0,
                     help="merge_path kernel: 0 warp-streaming, 1 CTA ring")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-row-scale", action="store_true",
+                    help="16-bit values without per-row scales")
     ap.add_argument("--n", type=int, default=128, help="SpMM: columns of B")
     ap.add_argument("--b-dtype", default="f32", choices=["f32", "bf16", "f16"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
