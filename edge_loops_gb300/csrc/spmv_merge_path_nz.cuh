@@ -58,7 +58,7 @@ struct __align__(16) WarpSmem {
   float yv[kMaxEnds];          // the tile's row sums (or, whole tiles, sums by end position)
   float yc[COMP ? kMaxEnds : 4];
   unsigned char kp[32][kPer];  // row end closed after lane l's product i (tile-local)
-  unsigned bits[8];            // whole tiles: bit p-1 = a row ends after nonzero p-1
+  unsigned mw[32];             // whole tiles: bit i of word l = a row ends after nonzero 8 l + i
   int pend;
   float pend_s, pend_c;
 };
@@ -192,7 +192,7 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
     }
   };
 
-  if (lane < 8) S.bits[lane] = 0u;
+  S.mw[lane] = 0u;
   int ra = rs, lo = ns;  // first row not yet closed; first nonzero of the tile
   int hi = tile_hi(lo);
   load_tile(lo, hi);
@@ -216,7 +216,7 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
         int pe = __shfl_up_sync(kFullMask, el, 1);
         if (lane == 0) pe = prev;
         if (lane < cnt) {
-          S.re[base + lane] = el;
+          if (base > 0) S.re[base + lane] = el;  // the first 32 stay in el0
           rising = rising && el > pe;
         }
         if (base == 0) el0 = el;
@@ -229,6 +229,7 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
       }
     }
     const bool fast = __all_sync(kFullMask, rising) && X < kMaxEnds && hi - lo == kTileNz;
+    if (!fast && lane < X) S.re[lane] = el0;
     __syncwarp();
     if (X >= kMaxEnds) hi = lo + S.re[kMaxEnds - 1];  // cut the tile at its 256th row end
     const int Y = hi - lo;
@@ -253,17 +254,19 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
 
     if (fast) {
       // Whole tile, strictly increasing row ends.  A lane's close bits come
-      // from a map of the end positions (bit p-1 of S.bits = a row ends
-      // after nonzero p-1); the lane's running sums are staged by position
-      // (S.yv[q] = its products since its previous close, up to nonzero q),
+      // from a word per lane that the end positions are OR-ed into (bit i
+      // of S.mw[l] = a row ends after nonzero 8 l + i); the lane's running
+      // sums are staged by position
+      // (its products since its previous close, up to nonzero q),
       // its tail is stitched by a segmented scan whose segment starts come
       // from one ballot, and row r's sum is read back at its end position.
       for (int kk = lane; kk < X; kk += 32) {
         const int P = kk < 32 ? el0 : S.re[kk];
-        if (P > 0) atomicOr(&S.bits[(P - 1) >> 5], 1u << ((P - 1) & 31));
+        if (P > 0) atomicOr(&S.mw[(P - 1) >> 3], 1u << ((P - 1) & 7));
       }
       __syncwarp();
-      const unsigned mask = (S.bits[lane >> 2] >> (kPer * (lane & 3))) & 0xffu;
+      const unsigned mask = S.mw[lane];
+      S.mw[lane] = 0u;  // only this lane reads it; the next tile writes it after a barrier
       Acc<COMP> run;
       float ss[kPer], sc[kPer];
 #pragma unroll
@@ -273,11 +276,11 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
         sc[i] = run.comp();
         if ((mask >> i) & 1u) run = Acc<COMP>();
       }
-      reinterpret_cast<float4*>(&S.yv[kPer * lane])[0] = make_float4(ss[0], ss[1], ss[2], ss[3]);
-      reinterpret_cast<float4*>(&S.yv[kPer * lane])[1] = make_float4(ss[4], ss[5], ss[6], ss[7]);
-      if (COMP) {
-        reinterpret_cast<float4*>(&S.yc[kPer * lane])[0] = make_float4(sc[0], sc[1], sc[2], sc[3]);
-        reinterpret_cast<float4*>(&S.yc[kPer * lane])[1] = make_float4(sc[4], sc[5], sc[6], sc[7]);
+      // position q lives at S.yv[(q % 8) * 32 + q / 8]: conflict-free stores
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
+        S.yv[32 * i + lane] = ss[i];
+        if (COMP) S.yc[32 * i + lane] = sc[i];
       }
       // a row closed at position 0 (before the tile's first nonzero) takes
       // the carry; otherwise the carry runs into the first lanes
@@ -304,7 +307,7 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
       if (lane == 0) ex = cin;
       const Acc<COMP> cout = shfl_idx_acc(inc, 31);
       if (mask) {  // the lane's first close: earlier parts of the row first
-        const int f = kPer * lane + __ffs(mask) - 1;
+        const int f = 32 * (__ffs(mask) - 1) + lane;
         Acc<COMP> mine;
         mine.set(S.yv[f], COMP ? S.yc[f] : 0.f);
         ex.add(mine);
@@ -312,11 +315,11 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
         if (COMP) S.yc[f] = ex.comp();
       }
       __syncwarp();
-      if (lane < 8) S.bits[lane] = 0u;  // every lane has read its mask
       for (int kk = lane; kk < X; kk += 32) {  // coalesced store of the tile's rows
         const int P = kk < 32 ? el0 : S.re[kk];
         Acc<COMP> val = carry;
-        if (P > 0) val.set(S.yv[P - 1], COMP ? S.yc[P - 1] : 0.f);
+        const int q = 32 * ((P - 1) & 7) + ((P - 1) >> 3);
+        if (P > 0) val.set(S.yv[q], COMP ? S.yc[q] : 0.f);
         const int r = ra + kk;
         if (need_lb && r == rs) {
           // the range's first row end closes row rs, begun in an earlier
