@@ -211,9 +211,8 @@ def run_ours(args, rank, world):
     times = [s.elapsed_time(e) for s, e in zip(starts, ends)]  # ms
     kern_ms = sum(times)
     if world > 1:
-        t = torch.tensor([kern_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        kern_ms = float(t.item())
+        from edge_loops_gb300.dist import max_over_ranks
+        kern_ms = max_over_ranks(kern_ms, device=dev)
     flags = ws.errors()
     if flags:
         raise SystemExit(f"device error flags {flags:#x} in the timed region")
@@ -381,13 +380,39 @@ def cpu_baseline(W, args, budget_s=15.0, threads=None):
         if len(times) >= 2000:
             break
     med = statistics.median(times)
+    # the reference runs its CPU check single-threaded: time that too (bounded)
+    one = []
+    t_end = time.perf_counter() + max(2.0, budget_s / 5)
+    while time.perf_counter() < t_end or len(one) < 3:
+        t0 = time.perf_counter()
+        oracle.spmv_f32(off, idx, vals, x)
+        one.append(time.perf_counter() - t0)
+        if len(one) >= 200:
+            break
+    med1 = statistics.median(one)
     return {"value": round(nbytes / med / 1e9, 3), "unit": "GB/s", "cores": threads,
+            "single_thread": {"value": round(nbytes / med1 / 1e9, 3), "unit": "GB/s",
+                              "ms_per_step": round(med1 * 1e3, 3), "repetitions": len(one)},
+            "cpu_model": _cpu_model(),
             "kind": "port",
             "sample": (f"whole matrix (FP32 values), {len(times)} repetitions in "
                        f"~{budget_s:.0f} s, median; reference loop examples/spmv/"
                        f"helpers.hxx:106-112 restated in oracle/oracle.c, rows split "
                        f"over {threads} threads"),
             "ms_per_step": round(med * 1e3, 3)}
+
+
+def _cpu_model():
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                low = line.lower()
+                if low.startswith("model name") or low.startswith("cpu part"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
 
 
 def run_reference(args, rank, world):
