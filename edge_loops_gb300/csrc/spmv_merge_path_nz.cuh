@@ -197,6 +197,8 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
   int hi = tile_hi(lo);
   load_tile(lo, hi);
   int o = load_ends(ra);
+  int o2 = 0;          // ends of the next 32 rows, when the last tile predicts them
+  bool has_o2 = false;
   gather();
   Acc<COMP> carry;
 
@@ -225,7 +227,7 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
         prev = __shfl_sync(kFullMask, el, 31);
         base += 32;
         const int k = ra + base + 1 + lane;
-        e = k <= rows ? __ldg(m.offsets + k) : 0x7fffffff;
+        e = base == 32 && has_o2 ? o2 : k <= rows ? __ldg(m.offsets + k) : 0x7fffffff;
       }
     }
     const bool fast = __all_sync(kFullMask, rising) && X < kMaxEnds && hi - lo == kTileNz;
@@ -251,6 +253,10 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
     const int lo2 = hi, hi2 = tile_hi(hi), ra2 = ra + X;
     if (lo2 < ne) load_tile(lo2, hi2);
     if (ra2 < re) o = load_ends(ra2);
+    // a tile with many row ends is likely followed by another: fetch the
+    // second window too, so that its ballot does not wait on a dependent load
+    has_o2 = X >= 24 && ra2 + 32 < re;
+    if (has_o2) o2 = load_ends(ra2 + 32);
 
     if (fast) {
       // Whole tile, strictly increasing row ends.  A lane's close bits come
