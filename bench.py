@@ -571,11 +571,12 @@ def run_batched(args):
     else:
         tdt = torch.bfloat16 if args.value_dtype == "bf16" else torch.float16
         yq = torch.empty_like(y32)
-        items = [(A.quantized(tdt, per_row_scale=True), x, yq[int(rs[m]): int(rs[m]) + A.rows])
+        items = [(A.quantized(tdt, per_row_scale=not args.no_row_scale), x,
+                  yq[int(rs[m]): int(rs[m]) + A.rows])
                  for m, (A, x, _) in enumerate(items32)]
         plan = api.BatchPlan(items)
         ms = _time_device(plan.execute, args.steps, args.warmup, flush, stream)
-        nb = total_bytes(items, 2, True)
+        nb = total_bytes(items, 2, not args.no_row_scale)
     if plan.errors() or plan32.errors():
         raise SystemExit("device error flags in the batched plan")
     # plain FP32 kernel, one launch per matrix
@@ -630,7 +631,8 @@ def run_batched(args):
                    "algorithmic_bytes_per_step": nb, "plan": plan.info(),
                    "l2": "flushed before every step (512 MiB write, outside the timed graph)"},
         "roofline": {"bound": "hbm", "achieved": round(ach, 2), "peak": peak, "unit": "GB/s",
-                     "frac": round(ach / peak, 4), "peak_source": kind, "traffic": None},
+                     "frac": round(ach / peak, 4), "peak_source": kind,
+                     "traffic": traffic_for(f"spmv_batched:{args.value_dtype}")},
         "comparison": {
             "batched_fp32_GBps": round(thr(b32, ms32), 2), "batched_fp32_ms": round(ms32, 4),
             "plain_fp32_per_matrix_graph_GBps": round(thr(b32, ms_plain), 2),
