@@ -176,6 +176,8 @@ def run_ours(args, rank, world):
     opts = dict(items_per_thread=args.ipt) if args.ipt else {}
     if args.variant:
         opts["variant"] = args.variant
+    if args.row_weight:
+        opts["row_weight"] = args.row_weight
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
 
@@ -658,6 +660,8 @@ def main():
     ap.add_argument("--ipt", type=int, default=0)
     ap.add_argument("--variant", type=int, default=0,
                     help="merge_path kernel: 0 warp-streaming, 1 CTA ring")
+    ap.add_argument("--row-weight", type=int, default=0,
+                    help="merge_path: merge items per row end in the warp split (0 = default)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-row-scale", action="store_true",
                     help="16-bit values without per-row scales")

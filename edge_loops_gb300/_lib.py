@@ -62,7 +62,8 @@ class ElSpmvOpts(C.Structure):
         ("wait_limit_us", C.c_int32),
         ("test_hooks", C.c_int32),
         ("variant", C.c_int32),
-        ("reserved", C.c_int32 * 5),
+        ("row_weight", C.c_int32),
+        ("reserved", C.c_int32 * 4),
     ]
 
 

@@ -47,6 +47,7 @@ struct Args {
   long long num_ranges;
   int vec_ok;             // 128-bit loads allowed at tile starts (tile_phase)
   int ph;                 // tile phase (tile_phase)
+  int rw;                 // merge items per row end (the ranges' split)
   int test_hooks;
   unsigned long long wait_ns;
   WsView ws;
@@ -457,24 +458,35 @@ __device__ __forceinline__ void run_range(const Args& a, SmemT& S, const int war
   WsHeader* hdr = a.ws.hdr;
   const float* __restrict__ scale = a.row_scale;
 
-  unsigned tk = 0, ep = 0;
-  if (lane == 0) {
-    tk = atomicAdd(&hdr->ticket, 1u);
-    ep = read_epoch(hdr);
+  // one ticket per CTA (its warps take ranges ticket * warps_per_cta + w):
+  // a range only waits on ranges of CTAs that took their ticket earlier and
+  // are therefore running
+  __shared__ unsigned s_ticket[2];
+  if (threadIdx.x == 0) {
+    s_ticket[0] = atomicAdd(&hdr->ticket, 1u);
+    s_ticket[1] = read_epoch(hdr);
   }
-  const long long g = __shfl_sync(kFullMask, tk, 0);
-  const unsigned epoch = __shfl_sync(kFullMask, ep, 0);
+  __syncthreads();
+  const long long g = (long long)s_ticket[0] * warps_per_cta + (threadIdx.x >> 5);
+  const unsigned epoch = s_ticket[1];
   const unsigned tag = epoch_tag(epoch);
-  const long long total = a.rows + a.nnz;
+  const long long w = a.rw;
+  const long long total = w * a.rows + a.nnz;
 
   if (g < a.num_ranges) {
+    // split points at diagonals g * range_items of the merge of row ends
+    // (w items each) and nonzeros
     const long long dd0 = g * a.range_items;
-    const int d0 = (int)(dd0 < total ? dd0 : total);
-    const int d1 = (int)(dd0 + a.range_items < total ? dd0 + a.range_items : total);
-    const int rs = (int)warp_merge_search(a.offsets + 1, a.rows, a.nnz, d0);
-    const int ns = d0 - rs;
-    const int re = (int)warp_merge_search(a.offsets + 1, a.rows, a.nnz, d1);
-    const int ne = d1 - re;
+    const long long d0 = dd0 < total ? dd0 : total;
+    const long long d1 = dd0 + a.range_items < total ? dd0 + a.range_items : total;
+    auto nz_of = [&](long long d, int r) {  // the diagonal's nonzero coordinate
+      const long long n = d - w * r;
+      return (int)((long long)r < a.rows ? min(n, (long long)__ldg(a.offsets + r + 1)) : n);
+    };
+    const int rs = (int)warp_merge_search_w(a.offsets + 1, a.rows, a.nnz, d0, w);
+    const int ns = nz_of(d0, rs);
+    const int re = (int)warp_merge_search_w(a.offsets + 1, a.rows, a.nnz, d1, w);
+    const int ne = nz_of(d1, re);
     const int off_rs = __ldg(a.offsets + rs);
     const bool need_lb = ns > off_rs;
     if (lane == 0) {
@@ -509,7 +521,7 @@ __device__ __forceinline__ void run_range(const Args& a, SmemT& S, const int war
     if (need_lb && S.pend) {
       // row rs began in range gfirst: sum the partials of ranges [gfirst, g)
       // in a fixed order
-      const long long gfirst = ((long long)rs + off_rs) / a.range_items;
+      const long long gfirst = (w * rs + off_rs) / a.range_items;
       Acc<COMP> acc;
       bool ok = true;
       for (long long kk = gfirst + lane; kk < g && kk < a.ws.nslots; kk += 32) {
@@ -552,12 +564,12 @@ __device__ __forceinline__ void run_range(const Args& a, SmemT& S, const int war
     }
   }
 
-  // the last warp to finish hands the workspace back for the next launch
-  if (lane == 0) {
+  // the last CTA to finish hands the workspace back for the next launch
+  __syncthreads();
+  if (threadIdx.x == 0) {
     __threadfence();
-    const unsigned total_warps = gridDim.x * (unsigned)warps_per_cta;
     const unsigned prev = atomicAdd(&hdr->done, 1u);
-    if (prev == total_warps - 1) finish_launch(hdr, epoch);
+    if (prev == gridDim.x - 1) finish_launch(hdr, epoch);
   }
 }
 
@@ -566,6 +578,18 @@ __global__ void __launch_bounds__(kTPB, 3)
     merge_path_nz_kernel(const Args a) {
   __shared__ WarpSmem<COMP> smem_all[kWarps];
   run_range<VT, COMP, NzWalk>(a, smem_all[threadIdx.x >> 5], kWarps);
+}
+
+// Merge items per row end for the warp ranges: a row end costs the walk
+// about as much as two nonzeros (its ballot, bit, staging and store), so
+// ranges of short rows get fewer items.  Falls back to 1 where the weighted
+// merge length would not fit 31 bits.
+constexpr int kDefaultRowWeight = 2;
+inline int row_weight(const SpmvCall& c) {
+  int w = c.o.row_weight > 0 ? c.o.row_weight : kDefaultRowWeight;
+  if (w > 16) w = 16;
+  if ((long long)w * c.A.rows + c.A.nnz >= (1LL << 31)) w = 1;
+  return w;
 }
 
 template <typename VT, bool COMP>
@@ -577,7 +601,8 @@ int resident_warps(int device) {
 
 template <typename VT, bool COMP>
 el_status launch(const SpmvCall& c) {
-  const long long total = c.A.rows + c.A.nnz;
+  const int rw = row_weight(c);
+  const long long total = (long long)rw * c.A.rows + c.A.nnz;
   // ranges of whole 256-item units, one per resident warp
   const long long units = (total + kTileNz - 1) / kTileNz;
   long long W = resident_warps<VT, COMP>(c.device);
@@ -598,6 +623,7 @@ el_status launch(const SpmvCall& c) {
   a.range_items = upr * kTileNz;
   a.num_ranges = (units + upr - 1) / upr;
   tile_phase(c.A.indices, c.A.values, (int)sizeof(VT), &a.vec_ok, &a.ph);
+  a.rw = rw;
   a.test_hooks = c.o.test_hooks;
   a.wait_ns = c.wait_ns;
   a.ws = c.ws;

@@ -44,7 +44,7 @@ template <typename VT>
 el_status launch_static(const el_csr& A, const float* x, float* y, int ranges, void* scratch,
                         int device, cudaStream_t stream) {
   using namespace mpn;
-  const long long total = A.rows + A.nnz;
+  const long long total = A.rows + A.nnz;  // the reference's equal split (row weight 1)
   const long long units = (total + kTileNz - 1) / kTileNz;
   long long W = ranges > 0 ? ranges : resident_warps<VT, false>(device);
   if (W > kStaticRanges) W = kStaticRanges;
@@ -64,6 +64,7 @@ el_status launch_static(const el_csr& A, const float* x, float* y, int ranges, v
   a.range_items = upr * kTileNz;
   a.num_ranges = (units + upr - 1) / upr;
   tile_phase(A.indices, A.values, (int)sizeof(VT), &a.vec_ok, &a.ph);
+  a.rw = 1;
   a.test_hooks = 0;
   a.wait_ns = 2000000000ull;
   a.ws.hdr = reinterpret_cast<WsHeader*>(scratch);

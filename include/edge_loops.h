@@ -144,7 +144,13 @@ typedef struct el_spmv_opts {
                                     items, lane t from the split point of
                                     diagonal 8t (the reference's per-thread
                                     split) */
-  int32_t reserved[5];
+  int32_t row_weight;        /* merge_path (variant 0): the warp ranges split
+                                the merge of row ends and nonzeros with a
+                                row end counted as this many nonzeros, so
+                                ranges of short rows hold fewer items; 0 =
+                                the library default, 1 = the reference's
+                                equal split */
+  int32_t reserved[4];
 } el_spmv_opts;
 
 typedef struct el_workspace el_workspace;

@@ -16,6 +16,8 @@ pytestmark = pytest.mark.gpu
 SCHEDS = [
     ("merge_path_flat", {}),
     ("merge_path_flat", {"compensated": True}),
+    ("merge_path_flat", {"row_weight": 1}),
+    ("merge_path_flat", {"row_weight": 5, "max_ctas": 3}),
     ("merge_path_flat", {"variant": 2}),
     ("merge_path_flat", {"variant": 2, "compensated": True}),
     ("merge_path_flat", {"variant": 1}),
@@ -155,6 +157,7 @@ def test_long_rows_across_many_ctas(cuda, oracle_mod):
                                    long_rows=[(0, 250_000), (17, 120_000), (399, 200_000)])
     A = dev_csr(off, idx, vals, 300_000, cuda)
     for opts in ({}, {"max_ctas": 3}, {"max_ctas": 1}, {"compensated": True},
+                 {"row_weight": 1}, {"row_weight": 7, "max_ctas": 2},
                  {"variant": 2}, {"variant": 2, "max_ctas": 1},
                  {"variant": 1, "items_per_thread": 4},
                  {"variant": 1, "items_per_thread": 4, "max_ctas": 7},
