@@ -333,6 +333,71 @@ __device__ __forceinline__ long long warp_merge_search_w(
   return lo + __popc(__ballot_sync(kFullMask, t));
 }
 
+// Two weighted split points at once (diagonals da and db, rows w items
+// each), with both searches' probes in flight together.  Also returns
+// offsets[x] and offsets[x+1] of each split row x (row_end = offsets + 1;
+// offsets[rows + 1] reads as nnz), taken from the final probes where they
+// hold them.
+struct SplitPoint {
+  long long x;  // rows closed before the diagonal
+  int start;    // offsets[x]
+  int end;      // offsets[x + 1] (nnz for x == rows)
+};
+__device__ __forceinline__ void warp_merge_search2_w(const int* __restrict__ row_end,
+                                                     long long rows, long long nnz,
+                                                     long long da, long long db, long long w,
+                                                     SplitPoint& A, SplitPoint& B) {
+  const int lane = threadIdx.x & 31;
+  long long lo[2], hi[2];
+  const long long d[2] = {da, db};
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    lo[k] = d[k] > nnz ? (d[k] - nnz) / w : 0;
+    hi[k] = d[k] / w;
+    if (lo[k] > rows) lo[k] = rows;
+    if (hi[k] > rows) hi[k] = rows;
+  }
+  while (hi[0] - lo[0] > 32 || hi[1] - lo[1] > 32) {  // warp-uniform
+    long long p[2];
+    int v[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      p[k] = lo[k] + ((long long)(lane + 1) * (hi[k] - lo[k])) / 33;
+      v[k] = hi[k] - lo[k] > 32 ? __ldg(row_end + p[k]) : 0;  // both loads before either use
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      if (hi[k] - lo[k] <= 32) continue;
+      const bool t = (long long)v[k] <= d[k] - w * (p[k] + 1);
+      const int c = __popc(__ballot_sync(kFullMask, t));
+      const long long plo = __shfl_sync(kFullMask, p[k], c > 0 ? c - 1 : 0);
+      const long long phi = __shfl_sync(kFullMask, p[k], c < 32 ? c : 31);
+      if (c > 0) lo[k] = plo + 1;
+      if (c < 32) hi[k] = phi;
+    }
+  }
+  long long p[2];
+  int v[2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    p[k] = lo[k] + lane;
+    v[k] = p[k] < hi[k] ? __ldg(row_end + p[k]) : 0;
+  }
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    SplitPoint& S = k == 0 ? A : B;
+    const bool t = p[k] < hi[k] && (long long)v[k] <= d[k] - w * (p[k] + 1);
+    const int c = __popc(__ballot_sync(kFullMask, t));
+    S.x = lo[k] + c;
+    // offsets[x + 1] = row_end[x] was probed by lane c (if x < hi), offsets[x]
+    // = row_end[x - 1] by lane c - 1 (if c > 0)
+    const int ve = __shfl_sync(kFullMask, v[k], c < 32 ? c : 31);
+    const int vs = __shfl_sync(kFullMask, v[k], c > 0 ? c - 1 : 0);
+    S.end = (S.x < hi[k] && c < 32) ? ve : S.x < rows ? __ldg(row_end + S.x) : (int)nnz;
+    S.start = c > 0 ? vs : S.x > 0 ? __ldg(row_end + S.x - 1) : __ldg(row_end - 1);
+  }
+}
+
 // ------------------------------------------------------ segmented scan
 // Operator of a segmented sum over items in order: (f1,v1) (+) (f2,v2) =
 // (f1|f2, f2 ? v2 : v1+v2), where f marks an item that starts a new

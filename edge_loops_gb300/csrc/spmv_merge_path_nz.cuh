@@ -479,15 +479,17 @@ __device__ __forceinline__ void run_range(const Args& a, SmemT& S, const int war
     const long long dd0 = g * a.range_items;
     const long long d0 = dd0 < total ? dd0 : total;
     const long long d1 = dd0 + a.range_items < total ? dd0 + a.range_items : total;
-    auto nz_of = [&](long long d, int r) {  // the diagonal's nonzero coordinate
-      const long long n = d - w * r;
-      return (int)((long long)r < a.rows ? min(n, (long long)__ldg(a.offsets + r + 1)) : n);
+    SplitPoint sa, sb;
+    warp_merge_search2_w(a.offsets + 1, a.rows, a.nnz, d0, d1, w, sa, sb);
+    auto nz_of = [&](long long d, const SplitPoint& sp) {  // the nonzero coordinate
+      const long long n = d - w * sp.x;
+      return (int)(sp.x < a.rows ? min(n, (long long)sp.end) : n);
     };
-    const int rs = (int)warp_merge_search_w(a.offsets + 1, a.rows, a.nnz, d0, w);
-    const int ns = nz_of(d0, rs);
-    const int re = (int)warp_merge_search_w(a.offsets + 1, a.rows, a.nnz, d1, w);
-    const int ne = nz_of(d1, re);
-    const int off_rs = __ldg(a.offsets + rs);
+    const int rs = (int)sa.x;
+    const int ns = nz_of(d0, sa);
+    const int re = (int)sb.x;
+    const int ne = nz_of(d1, sb);
+    const int off_rs = sa.start;
     const bool need_lb = ns > off_rs;
     if (lane == 0) {
       S.pend = 0;
@@ -506,7 +508,7 @@ __device__ __forceinline__ void run_range(const Args& a, SmemT& S, const int war
 
     // range end (re, ne): publish the partial of the row still open, if this
     // range holds any of its nonzeros; exactly one later range reads it
-    const int off_re = __ldg(a.offsets + re);
+    const int off_re = sb.start;
     if (lane == 0) {
       if ((long long)re == a.rows && (long long)off_re != a.nnz)
         raise_flag(hdr, EL_FLAG_NNZ_MISMATCH, (unsigned)re);
