@@ -125,6 +125,8 @@ SIGNATURES = {
     "el_batch_plan_destroy": (C.c_int, [C.c_void_p]),
     "el_spmv_static_scratch": (C.c_int, [C.POINTER(ElCsr), C.c_void_p, C.c_void_p, C.c_int32,
                                          C.POINTER(C.c_uint32), C.c_void_p]),
+    "el_spmv_host": (C.c_int, [C.c_void_p, C.POINTER(ElCsr), C.c_int32, C.POINTER(ElSpmvOpts),
+                               C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
 }
 
 EL_STATIC_MAX_RANGES = 4096

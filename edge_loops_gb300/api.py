@@ -180,6 +180,28 @@ def spmv(A, x, y=None, schedule="merge_path_flat", stream=None, workspace=None, 
     return y
 
 
+def spmv_host(A, x, y=None, schedule="merge_path_flat", block_nnz=0, stream=None,
+              workspace=None, **opts):
+    """el_spmv_host: y = A x with A (CSR of CPU tensors), x and y in host
+    memory, streamed to the current GPU in row blocks that overlap the copies
+    with the SpMV.  Pin the tensors (`.pin_memory()`) for full link speed.
+    Asynchronous: synchronise the stream before reading y or reusing A, x."""
+    if A.offsets.is_cuda or x.is_cuda:
+        raise ValueError("spmv_host takes host (CPU) tensors")
+    if y is None:
+        y = torch.empty(A.rows, dtype=torch.float32).pin_memory()
+    if x.dtype != torch.float32 or y.dtype != torch.float32 or y.is_cuda:
+        raise TypeError("x and y are float32 host tensors")
+    if x.numel() < A.cols or y.numel() < A.rows:
+        raise ValueError("x or y too short")
+    a = A.el()
+    o = make_opts(**opts)
+    L.check(L.lib().el_spmv_host(_ws(workspace), C.byref(a), _sched(schedule), C.byref(o),
+                                 _ptr(x), _ptr(y), int(block_nnz), _stream(stream)),
+            "el_spmv_host")
+    return y
+
+
 def spmm(A, B, Cm=None, schedule="merge_path_flat", stream=None, workspace=None, **opts):
     """C = A B with B row-major (cols x n) float32/bfloat16/float16 and C
     float32 (rows x n), the reference's loops::algorithms::spmm."""

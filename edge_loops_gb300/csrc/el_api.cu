@@ -17,6 +17,11 @@ struct el_workspace {
   long long nslots;
   void* scratch;  // row-vector carries of the merge-path SpMM
   size_t scratch_bytes;
+  // el_spmv_host: device staging memory, a copy stream and its events
+  void* stage = nullptr;
+  size_t stage_bytes = 0;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t events[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 namespace el {
@@ -197,6 +202,38 @@ el_status resolve_ws(el_workspace* ws, cudaStream_t stream, int device,
 
 WsView workspace_view(el_workspace* ws) { return ws_view(ws); }
 
+el_status workspace_resolve(el_workspace* ws, cudaStream_t stream, int device,
+                            el_workspace** out) {
+  return resolve_ws(ws, stream, device, out);
+}
+
+el_status workspace_stage(el_workspace* ws, size_t bytes, void** stage,
+                          cudaStream_t* copy_stream, cudaEvent_t* events) {
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != ws->device) return fail(EL_ERR_INVALID_ARGUMENT, "workspace of another device");
+  cudaError_t e = cudaSuccess;
+  if (!ws->copy_stream) {
+    e = cudaStreamCreateWithFlags(&ws->copy_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_status(e, "copy stream");
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i)
+      e = cudaEventCreateWithFlags(&ws->events[i], cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_status(e, "copy events");
+  }
+  if (bytes > ws->stage_bytes) {
+    if (ws->stage) cudaFree(ws->stage);  // waits for the device
+    ws->stage = nullptr;
+    ws->stage_bytes = 0;
+    e = cudaMalloc(&ws->stage, bytes);
+    if (e != cudaSuccess) return cuda_status(e, "staging memory");
+    ws->stage_bytes = bytes;
+  }
+  *stage = ws->stage;
+  *copy_stream = ws->copy_stream;
+  for (int i = 0; i < 4; ++i) events[i] = ws->events[i];
+  return EL_OK;
+}
+
 el_status workspace_prepare(el_workspace* ws, const el_csr& A, int schedule) {
   SpmvCall c;
   c.A = A;
@@ -262,6 +299,10 @@ el_status el_workspace_destroy(el_workspace* ws) {
   if (!ws) return EL_OK;
   if (ws->dev) cudaFree(ws->dev);
   if (ws->scratch) cudaFree(ws->scratch);
+  if (ws->stage) cudaFree(ws->stage);
+  for (int i = 0; i < 4; ++i)
+    if (ws->events[i]) cudaEventDestroy(ws->events[i]);
+  if (ws->copy_stream) cudaStreamDestroy(ws->copy_stream);
   delete ws;
   return EL_OK;
 }

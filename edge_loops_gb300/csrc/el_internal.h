@@ -78,6 +78,13 @@ long long spmm_slots_needed(const SpmmCall& c, int schedule);
 WsView workspace_view(el_workspace* ws);
 // Sizes `ws` for an SpMV of A with `schedule` (default options).
 el_status workspace_prepare(el_workspace* ws, const el_csr& A, int schedule);
+// The caller's workspace or the library's one for (device, stream).
+el_status workspace_resolve(el_workspace* ws, cudaStream_t stream, int device,
+                            el_workspace** out);
+// At least `bytes` of device staging memory in `ws` (reallocated, which
+// waits for the device, when it grows), plus its copy stream and 4 events.
+el_status workspace_stage(el_workspace* ws, size_t bytes, void** stage,
+                          cudaStream_t* copy_stream, cudaEvent_t* events);
 
 el_status launch_partition_tiles(const int32_t* offsets, int64_t rows,
                                  int64_t nnz, int64_t items,

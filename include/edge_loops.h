@@ -180,6 +180,22 @@ el_status el_spmv(el_workspace* ws, const el_csr* A, int32_t schedule,
                   const el_spmv_opts* opts, const float* x, float* y,
                   el_stream_t stream);
 
+/* y = A x with the CSR arrays, row scales, x and y in HOST memory (no
+ * counterpart in the reference).  The rows are cut into blocks of about
+ * block_nnz nonzeros (0 = nnz / 2 clamped to [2^22, 2^27]); each block is
+ * copied to device staging memory of the workspace on a copy stream while
+ * the previous block is multiplied on `stream`, and its y rows are copied
+ * back.  Pinned host memory gives full link speed; the device holds x, y
+ * and two blocks at a time, so the matrix may exceed device memory.  The
+ * host offsets must start at 0, end at nnz and not decrease between blocks
+ * (EL_ERR_MALFORMED_CSR).  Asynchronous on `stream`: y is complete, and the
+ * host arrays may be reused, once the stream has been synchronised.  Same
+ * results as el_spmv within the FP32 bound (block borders change the merge
+ * ranges). */
+el_status el_spmv_host(el_workspace* ws, const el_csr* A, int32_t schedule,
+                       const el_spmv_opts* opts, const float* x, float* y,
+                       int64_t block_nnz, el_stream_t stream);
+
 /* C = A B.  B is row-major A->cols x n (leading dimension ldb >= n) of
  * b_dtype (FP32 / BF16 / FP16); C is row-major FP32 A->rows x n (ldc >= n).
  * Schedules: THREAD_MAPPED (the reference's), GROUP_MAPPED (a warp per

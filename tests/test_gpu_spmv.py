@@ -289,3 +289,51 @@ def test_lookback_wait_times_out_with_status(cuda):
     assert ws.errors() & 0x8
     api.spmv(A, xt, y, workspace=ws, items_per_thread=4)
     assert ws.errors() == 0
+
+
+@pytest.mark.parametrize("block_nnz", [0, 5000, 7])
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+def test_spmv_host_streams_blocks(cuda, oracle_mod, block_nnz, dtype):
+    """el_spmv_host: CSR, x and y in (pinned) host memory, row blocks copied
+    while the previous block is multiplied; blocks smaller than a row give
+    one-row blocks."""
+    from edge_loops_gb300 import api
+    rng = np.random.default_rng(31)
+    off, idx, vals, x = random_csr(rng, rows=4000, cols=6000, max_len=60, empty_frac=0.1,
+                                   long_rows=[(11, 5000), (3999, 900)])
+    A = api.CSR(torch.as_tensor(off).pin_memory(), torch.as_tensor(idx).pin_memory(),
+                torch.as_tensor(vals).pin_memory(), len(off) - 1, len(x))
+    scale = None
+    if dtype != torch.float32:
+        Ad = A.__class__(A.offsets.to(cuda), A.indices.to(cuda), A.values.to(cuda), A.rows, A.cols)
+        Aq = Ad.quantized(dtype, per_row_scale=True)
+        A = api.CSR(A.offsets, A.indices, Aq.values.cpu().pin_memory(), A.rows, A.cols,
+                    row_scale=Aq.row_scale.cpu().pin_memory())
+        scale = A.row_scale.numpy()
+    xh = torch.as_tensor(x).pin_memory()
+    y = torch.full((A.rows,), float("nan")).pin_memory()
+    ws = api.Workspace()
+    for _ in range(2):  # the second call reuses the staging memory
+        api.spmv_host(A, xh, y, block_nnz=block_nnz, workspace=ws)
+        torch.cuda.synchronize()
+    assert ws.errors() == 0
+    check_against_oracle(oracle_mod, off, idx, A.values.float().numpy(), x, y.numpy(),
+                         scale=scale)
+
+
+def test_spmv_host_pageable_and_malformed(cuda, oracle_mod):
+    from edge_loops_gb300 import api, _lib
+    rng = np.random.default_rng(32)
+    off, idx, vals, x = random_csr(rng, rows=700, cols=800, max_len=30)
+    A = api.CSR(torch.as_tensor(off), torch.as_tensor(idx), torch.as_tensor(vals),
+                len(off) - 1, len(x))
+    y = api.spmv_host(A, torch.as_tensor(x), torch.empty(A.rows), block_nnz=999)
+    torch.cuda.synchronize()
+    check_against_oracle(oracle_mod, off, idx, vals, x, y.numpy())
+    bad = off.copy()
+    bad[-1] += 3  # offsets[rows] != nnz
+    B = api.CSR(torch.as_tensor(bad), torch.as_tensor(idx), torch.as_tensor(vals),
+                len(off) - 1, len(x))
+    with pytest.raises(_lib.ElError) as e:
+        api.spmv_host(B, torch.as_tensor(x))
+    assert e.value.status == _lib.EL_ERR_MALFORMED_CSR
