@@ -47,10 +47,10 @@ extern "C" el_status el_spmv_host(el_workspace* ws, const el_csr* A, int32_t sch
     return fail(EL_ERR_MALFORMED_CSR, "offsets[0] = %d, offsets[rows] = %d, nnz = %lld", off[0],
                 off[A->rows], (long long)A->nnz);
 
-  // blocks of whole rows, about `target` nonzeros each (at least one row)
-  // default: two blocks (each block costs a few copies, a launch and two
-  // stream hand-offs; the host link, not the SpMV, bounds the whole), at
-  // least 2^22 and at most 2^27 nonzeros each
+  // blocks of whole rows, about `target` nonzeros each (at least one row);
+  // by default two blocks of 2^22 .. 2^27 nonzeros: every block costs a few
+  // copies, a launch and two stream hand-offs, and the host link, not the
+  // SpMV, bounds the whole
   long long target = block_nnz > 0 ? block_nnz : (A->nnz + 1) / 2;
   if (block_nnz == 0) target = std::min(std::max(target, 1LL << 22), 1LL << 27);
   std::vector<long long> cut{0};
