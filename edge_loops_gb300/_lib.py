@@ -20,6 +20,8 @@ EL_ERR_MALFORMED_CSR = 5
 EL_ERR_CUDA = 6
 EL_ERR_OUT_OF_MEMORY = 7
 EL_ERR_DEVICE = 8
+EL_ERR_IO = 9
+EL_ERR_PARSE = 10
 
 EL_F32, EL_BF16, EL_F16 = 0, 1, 2
 
@@ -47,6 +49,17 @@ class ElCsr(C.Structure):
         ("value_dtype", C.c_int32),
         ("reserved0", C.c_int32),
         ("row_scale", C.c_void_p),
+    ]
+
+
+class ElCoo(C.Structure):
+    _fields_ = [
+        ("rows", C.c_int64),
+        ("cols", C.c_int64),
+        ("nnz", C.c_int64),
+        ("row_indices", C.c_void_p),
+        ("col_indices", C.c_void_p),
+        ("values", C.c_void_p),
     ]
 
 
@@ -127,6 +140,10 @@ SIGNATURES = {
                                          C.POINTER(C.c_uint32), C.c_void_p]),
     "el_spmv_host": (C.c_int, [C.c_void_p, C.POINTER(ElCsr), C.c_int32, C.POINTER(ElSpmvOpts),
                                C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
+    "el_read_matrix_market": (C.c_int, [C.c_char_p, C.POINTER(ElCoo)]),
+    "el_coo_free": (None, [C.POINTER(ElCoo)]),
+    "el_csr_from_coo": (C.c_int, [C.c_void_p, C.POINTER(ElCoo), C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_void_p]),
 }
 
 EL_STATIC_MAX_RANGES = 4096

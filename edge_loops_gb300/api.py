@@ -9,6 +9,7 @@ entry points of include/loops/algorithms/spmv/*.cuh): "merge_path_flat"
 "group_mapped", plus "auto".
 """
 import ctypes as C
+import os
 
 import torch
 
@@ -200,6 +201,54 @@ def spmv_host(A, x, y=None, schedule="merge_path_flat", block_nnz=0, stream=None
                                  _ptr(x), _ptr(y), int(block_nnz), _stream(stream)),
             "el_spmv_host")
     return y
+
+
+def read_matrix_market(path):
+    """el_read_matrix_market: (rows, cols, row_indices, col_indices, values)
+    of a MatrixMarket coordinate file as numpy arrays (0-based; symmetric
+    files with their mirrored entries), the reference's
+    matrix_market_t::load."""
+    import numpy as np
+    coo = L.ElCoo()
+    L.check(L.lib().el_read_matrix_market(os.fsencode(path), C.byref(coo)),
+            "el_read_matrix_market")
+    try:
+        n = int(coo.nnz)
+        def arr(ptr, ctype, dtype):
+            if n == 0:
+                return np.zeros(0, dtype=dtype)
+            return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ctype)), shape=(n,)).copy()
+        ri = arr(coo.row_indices, C.c_int32, np.int32)
+        ci = arr(coo.col_indices, C.c_int32, np.int32)
+        vv = arr(coo.values, C.c_float, np.float32)
+        return int(coo.rows), int(coo.cols), ri, ci, vv
+    finally:
+        L.lib().el_coo_free(C.byref(coo))
+
+
+def csr_from_coo(rows, cols, row_indices, col_indices, values, device=None, stream=None,
+                 workspace=None):
+    """el_csr_from_coo: a CSR (device) from COO entries (tensors or arrays,
+    copied to the device), sorted by (row, column) with duplicates kept in
+    input order, the reference's csr_t(coo_t)."""
+    dev = torch.device(device) if device is not None else torch.device(
+        "cuda", torch.cuda.current_device())
+    ri = torch.as_tensor(row_indices, dtype=torch.int32).to(dev).contiguous()
+    ci = torch.as_tensor(col_indices, dtype=torch.int32).to(dev).contiguous()
+    vv = torch.as_tensor(values, dtype=torch.float32).to(dev).contiguous()
+    nnz = int(ri.numel())
+    off = torch.empty(int(rows) + 1, dtype=torch.int32, device=dev)
+    idx = torch.empty(nnz, dtype=torch.int32, device=dev)
+    val = torch.empty(nnz, dtype=torch.float32, device=dev)
+    coo = L.ElCoo()
+    coo.rows, coo.cols, coo.nnz = int(rows), int(cols), nnz
+    coo.row_indices = ri.data_ptr() if nnz else None
+    coo.col_indices = ci.data_ptr() if nnz else None
+    coo.values = vv.data_ptr() if nnz else None
+    L.check(L.lib().el_csr_from_coo(_ws(workspace), C.byref(coo), _ptr(off),
+                                    _ptr(idx) if nnz else None, _ptr(val) if nnz else None,
+                                    _stream(stream)), "el_csr_from_coo")
+    return CSR(off, idx, val, int(rows), int(cols))
 
 
 def spmm(A, B, Cm=None, schedule="merge_path_flat", stream=None, workspace=None, **opts):

@@ -268,6 +268,8 @@ const char* el_status_string(el_status s) {
     case EL_ERR_CUDA: return "EL_ERR_CUDA";
     case EL_ERR_OUT_OF_MEMORY: return "EL_ERR_OUT_OF_MEMORY";
     case EL_ERR_DEVICE: return "EL_ERR_DEVICE";
+    case EL_ERR_IO: return "EL_ERR_IO";
+    case EL_ERR_PARSE: return "EL_ERR_PARSE";
   }
   return "EL_ERR_UNKNOWN";
 }

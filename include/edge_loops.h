@@ -72,7 +72,9 @@ typedef enum el_status {
   EL_ERR_MALFORMED_CSR = 5,    /* el_csr_validate found a defect */
   EL_ERR_CUDA = 6,             /* a CUDA runtime call failed */
   EL_ERR_OUT_OF_MEMORY = 7,    /* workspace allocation failed */
-  EL_ERR_DEVICE = 8            /* a kernel reported an error flag */
+  EL_ERR_DEVICE = 8,           /* a kernel reported an error flag */
+  EL_ERR_IO = 9,               /* a file could not be opened or read */
+  EL_ERR_PARSE = 10            /* a MatrixMarket file is malformed */
 } el_status;
 
 /* Value storage types.  Accumulation is FP32 for all of them. */
@@ -195,6 +197,34 @@ el_status el_spmv(el_workspace* ws, const el_csr* A, int32_t schedule,
 el_status el_spmv_host(el_workspace* ws, const el_csr* A, int32_t schedule,
                        const el_spmv_opts* opts, const float* x, float* y,
                        int64_t block_nnz, el_stream_t stream);
+
+/* ---- matrix ingest (the step before the path) ------------------------ */
+/* A matrix in coordinate form: nnz (row, column, value) entries, 0-based. */
+typedef struct el_coo {
+  int64_t rows, cols, nnz;
+  int32_t* row_indices;
+  int32_t* col_indices;
+  float* values;
+} el_coo;
+
+/* Reads a MatrixMarket coordinate file (real / integer / pattern; general,
+ * symmetric -- mirrored entries added --, skew-symmetric, hermitian read as
+ * written) into host arrays allocated with malloc, released by
+ * el_coo_free.  Replaces the reference's matrix_market_t::load
+ * (include/loops/container/market.hxx:99-227), returning EL_ERR_IO /
+ * EL_ERR_PARSE / EL_ERR_UNSUPPORTED instead of exiting. */
+el_status el_read_matrix_market(const char* path, el_coo* out);
+void el_coo_free(el_coo* coo);
+
+/* CSR from a COO whose arrays are in device memory: entries sorted by
+ * (row, column) -- stable, so duplicates keep their order and are all kept,
+ * as the reference keeps them --, offsets (rows + 1), indices and values
+ * (nnz each) written to caller-allocated device arrays.  Replaces
+ * csr_t(coo_t) (include/loops/container/csr.hxx:86-94).  An entry outside
+ * the matrix gives EL_ERR_MALFORMED_CSR (checked first: synchronises
+ * `stream` once); the rest is asynchronous. */
+el_status el_csr_from_coo(el_workspace* ws, const el_coo* coo, int32_t* offsets,
+                          int32_t* indices, float* values, el_stream_t stream);
 
 /* C = A B.  B is row-major A->cols x n (leading dimension ldb >= n) of
  * b_dtype (FP32 / BF16 / FP16); C is row-major FP32 A->rows x n (ldc >= n).

@@ -12,7 +12,8 @@ LIB = os.path.join(HERE, "liboracle.so")
 __all__ = [
     "build", "spmv_f32", "spmv_f32_mt", "spmv_f64", "spmm_f32", "spmm_f64", "mp_search",
     "merge_path_tile_coords", "merge_path_thread_coords", "merge_path_walk",
-    "work_oriented_coords", "group_mapped_map", "error_metrics",
+    "work_oriented_coords", "group_mapped_map", "error_metrics", "matrix_market_coo",
+    "csr_from_coo",
 ]
 
 
@@ -192,3 +193,43 @@ def error_metrics(y, y64, yabs):
     ninf = float(np.max(np.abs(y64))) if len(d) else 0.0
     norm = float(np.max(d) / ninf) if ninf > 0 else float(np.max(d) if len(d) else 0.0)
     return comp, norm
+
+
+def matrix_market_coo(path):
+    """The reference's MatrixMarket loader restated
+    (include/loops/container/market.hxx:99-227): coordinate files, real /
+    integer / pattern (value 1.0), 1-based -> 0-based, values read as double
+    and stored as float32; for "symmetric" every off-diagonal entry is
+    followed by its mirror (market.hxx:195-221).  Returns (rows, cols,
+    row_indices, col_indices, values)."""
+    with open(path) as f:
+        banner = f.readline().split()
+        field, symmetry = banner[3].lower(), banner[4].lower()
+        lines = [ln for ln in f if ln.strip() and not ln.lstrip().startswith("%")]
+    rows, cols, n = (int(t) for t in lines[0].split()[:3])
+    ri, ci, vv = [], [], []
+    for ln in lines[1:1 + n]:
+        t = ln.split()
+        i, j = int(t[0]) - 1, int(t[1]) - 1
+        v = 1.0 if field == "pattern" else float(t[2])
+        ri.append(i)
+        ci.append(j)
+        vv.append(v)
+        if symmetry == "symmetric" and i != j:
+            ri.append(j)
+            ci.append(i)
+            vv.append(v)
+    return (rows, cols, np.array(ri, dtype=np.int32), np.array(ci, dtype=np.int32),
+            np.array(vv, dtype=np.float64).astype(np.float32))
+
+
+def csr_from_coo(rows, row_indices, col_indices, values):
+    """The reference's CSR construction restated (container/csr.hxx:86-94):
+    sort the entries by (row, column) (coo.hxx:104-113; a stable sort here,
+    so equal entries keep their order), indices and values in that order,
+    offsets[r] = lower_bound(sorted rows, r) (detail/convert.hxx:75-77)."""
+    ri = np.asarray(row_indices, dtype=np.int64)
+    ci = np.asarray(col_indices, dtype=np.int64)
+    order = np.lexsort((ci, ri))  # stable
+    offsets = np.searchsorted(ri[order], np.arange(rows + 1), side="left").astype(np.int32)
+    return offsets, ci[order].astype(np.int32), np.asarray(values, dtype=np.float32)[order]
