@@ -331,11 +331,21 @@ el_status launch_typed(const SpmmCall& c, int schedule) {
 
 }  // namespace spmm
 
-// Ranges the merge-path SpMM may use: one per resident warp.
+// Ranges the merge-path SpMM may use: one per resident warp of the kernel
+// (of either column width) that fits most CTAs on an SM.
 static long long spmm_mp_ranges(const SpmmCall& c) {
-  const int per_sm = resident_ctas_per_sm(
-      (const void*)spmm::merge_path_kernel<float, float, 4>, 256, 0);
-  return (long long)(per_sm > 0 ? per_sm : 1) * device_info(c.device).sm_count * 8;
+  int per_sm = 1;
+  const void* kerns[] = {(const void*)spmm::merge_path_kernel<float, float, 4>,
+                         (const void*)spmm::merge_path_kernel<float, float, 1>,
+                         (const void*)spmm::merge_path_kernel<float, __nv_bfloat16, 4>,
+                         (const void*)spmm::merge_path_kernel<float, __nv_bfloat16, 1>,
+                         (const void*)spmm::merge_path_kernel<__nv_bfloat16, float, 1>,
+                         (const void*)spmm::merge_path_kernel<__half, __half, 1>};
+  for (const void* k : kerns) {
+    const int p = resident_ctas_per_sm(k, 256, 0);
+    if (p > per_sm) per_sm = p;
+  }
+  return (long long)per_sm * device_info(c.device).sm_count * 8;
 }
 
 size_t spmm_scratch_bytes(const SpmmCall& c, int schedule) {
