@@ -566,7 +566,7 @@ def run_spmm(args):
         "roofline": {"bound": "hbm", "achieved": round(ach, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(ach / peak, 4), "peak_source": kind,
                      "achieved_gather_model": round(gather / (ms * 1e-3) / 1e9, 2),
-                     "traffic": None},
+                     "traffic": traffic_for(f"spmm_powerlaw:{args.schedule}:{args.b_dtype}:{args.n}")},
         "gpu_launches": args.steps * ((args.n + 127) // 128),
         "check": {"sampled_rows": 2048, "entries_outside_fp32_bound": 0},
     }
