@@ -103,6 +103,49 @@ __device__ __forceinline__ float ld_val(const VT* p) {
   return to_f32(*p);
 }
 
+// A lane's 8 values of the tile in flight.  16-bit values stay packed as
+// loaded (4 words) and are widened only when the products are formed, so no
+// instruction waits on the load before then.
+template <typename VT>
+struct TileVals {
+  float v[kPer];
+  __device__ __forceinline__ void load_vec(const float* p) { load8(p, v); }
+  __device__ __forceinline__ void load_at(int i, const float* p) { v[i] = ld_val(p); }
+  __device__ __forceinline__ void zero_at(int i) { v[i] = 0.f; }
+  __device__ __forceinline__ float get(int i) const { return v[i]; }
+};
+template <typename H>
+struct TileVals16 {
+  uint32_t w[kPer / 2];
+  __device__ __forceinline__ void load_vec(const H* p) {
+    const uint4 u = __ldcs(reinterpret_cast<const uint4*>(p));
+    w[0] = u.x; w[1] = u.y; w[2] = u.z; w[3] = u.w;
+  }
+  __device__ __forceinline__ void put(int i, unsigned short h) {
+    w[i >> 1] = (i & 1) ? ((w[i >> 1] & 0xffffu) | ((uint32_t)h << 16))
+                        : ((w[i >> 1] & 0xffff0000u) | h);
+  }
+  __device__ __forceinline__ void load_at(int i, const H* p) {
+    put(i, __ldcs(reinterpret_cast<const unsigned short*>(p)));
+  }
+  __device__ __forceinline__ void zero_at(int i) { put(i, 0); }
+  __device__ __forceinline__ unsigned short half_at(int i) const {
+    return (unsigned short)((i & 1) ? (w[i >> 1] >> 16) : (w[i >> 1] & 0xffffu));
+  }
+};
+template <>
+struct TileVals<__nv_bfloat16> : TileVals16<__nv_bfloat16> {
+  __device__ __forceinline__ float get(int i) const {
+    return __uint_as_float((uint32_t)half_at(i) << 16);
+  }
+};
+template <>
+struct TileVals<__half> : TileVals16<__half> {
+  __device__ __forceinline__ float get(int i) const {
+    return __half2float(__ushort_as_half(half_at(i)));
+  }
+};
+
 // One matrix as the tile walk sees it.
 struct Src {
   const int* offsets;
@@ -153,22 +196,22 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
     return t < (unsigned)ne ? (int)t : ne;
   };
   int c[kPer];
-  float v[kPer];
+  TileVals<VT> v;
   auto load_tile = [&](int l, int h) {
     const int j0 = l + kPer * lane;
     if (m.vec_ok && h - l == kTileNz && ((l + m.ph) & 7) == 0) {
       load8i(m.indices + j0, c);
-      load8(vals + j0, v);
+      v.load_vec(vals + j0);
     } else {
 #pragma unroll
       for (int i = 0; i < kPer; ++i) {
         const int j = j0 + i;
         if (j < h) {
           c[i] = __ldcs(m.indices + j);
-          v[i] = ld_val(vals + j);
+          v.load_at(i, vals + j);
         } else {
           c[i] = -1;
-          v[i] = 0.f;
+          v.zero_at(i);
         }
       }
     }
@@ -245,10 +288,10 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
     float p[kPer];
     if (fast) {
 #pragma unroll
-      for (int i = 0; i < kPer; ++i) p[i] = __fmul_rn(v[i], xg[i]);
+      for (int i = 0; i < kPer; ++i) p[i] = __fmul_rn(v.get(i), xg[i]);
     } else {
 #pragma unroll
-      for (int i = 0; i < kPer; ++i) p[i] = kPer * lane + i < Y ? __fmul_rn(v[i], xg[i]) : 0.f;
+      for (int i = 0; i < kPer; ++i) p[i] = kPer * lane + i < Y ? __fmul_rn(v.get(i), xg[i]) : 0.f;
     }
     // the window registers are free: start loading the next tile
     const int lo2 = hi, hi2 = tile_hi(hi), ra2 = ra + X;
