@@ -275,6 +275,9 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
       }
     }
     const bool fast = __all_sync(kFullMask, rising) && X < kMaxEnds && hi - lo == kTileNz;
+    // row scales of the tile's first 32 rows: loaded now, used by the store
+    // at the end of the tile
+    const float sc0 = scale && lane < X ? __ldg(scale + ra + lane) : 1.f;
     if (!fast && lane < X) S.re[lane] = el0;
     __syncwarp();
     if (X >= kMaxEnds) hi = lo + S.re[kMaxEnds - 1];  // cut the tile at its 256th row end
@@ -380,7 +383,7 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
           continue;
         }
         float vv = val.value();
-        if (scale) vv *= __ldg(scale + r);
+        if (scale) vv *= kk < 32 ? sc0 : __ldg(scale + r);
         m.y[r] = vv;
       }
       carry = cout;
@@ -463,7 +466,7 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
         const int r = ra + kk;
         if (need_lb && r == rs) continue;
         float vv = COMP ? __fadd_rn(S.yv[kk], S.yc[kk]) : S.yv[kk];
-        if (scale) vv *= __ldg(scale + r);
+        if (scale) vv *= kk < 32 ? sc0 : __ldg(scale + r);
         m.y[r] = vv;
       }
       carry = shfl_idx_acc(seg_combine(cin, inc).v, 31);
