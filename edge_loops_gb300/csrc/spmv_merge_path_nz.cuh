@@ -64,32 +64,12 @@ struct __align__(16) WarpSmem {
   float pend_s, pend_c;
 };
 
-// 8 consecutive values (16-byte aligned for float: two 128-bit loads; one
-// for 16-bit types), converted to float.
+// 8 consecutive FP32 values (16-byte aligned: two 128-bit loads).
 __device__ __forceinline__ void load8(const float* p, float (&v)[kPer]) {
   const float4 a = __ldcs(reinterpret_cast<const float4*>(p));
   const float4 b = __ldcs(reinterpret_cast<const float4*>(p) + 1);
   v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
   v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-}
-__device__ __forceinline__ void load8(const __nv_bfloat16* p, float (&v)[kPer]) {
-  const uint4 u = __ldcs(reinterpret_cast<const uint4*>(p));
-  const unsigned w[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    v[2 * i] = __uint_as_float(w[i] << 16);
-    v[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
-  }
-}
-__device__ __forceinline__ void load8(const __half* p, float (&v)[kPer]) {
-  const uint4 u = __ldcs(reinterpret_cast<const uint4*>(p));
-  const unsigned w[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const __half2 h = *reinterpret_cast<const __half2*>(&w[i]);
-    v[2 * i] = __low2float(h);
-    v[2 * i + 1] = __high2float(h);
-  }
 }
 __device__ __forceinline__ void load8i(const int* p, int (&c)[kPer]) {
   const int4 a = __ldcs(reinterpret_cast<const int4*>(p));
