@@ -28,11 +28,20 @@
  *       [include/loops/schedule/merge_path_flat.hxx:108-138, :321-385]
  *   el_work_oriented_partition
  *       setup<work_oriented>::init [include/loops/schedule/work_oriented.hxx:150-167]
+ *   el_read_matrix_market / el_csr_from_coo
+ *       matrix_market_t::load and csr_t(coo_t)
+ *       [include/loops/container/market.hxx:99-227, csr.hxx:86-94]
+ * and adds entry points the reference does not have: el_spmv_host (matrix,
+ * x and y in host memory, streamed), el_spmv_static_scratch (no device
+ * allocation), the batched plan (el_batch_plan_*), el_quantize_values and
+ * el_csr_validate.  include/edge_loops_device.cuh holds the device-side
+ * load-balanced loop API for user kernels (the reference's schedule::setup).
  *
  * Conventions (differences from the reference are deliberate and listed):
  *   - Every call is asynchronous on the given stream (the reference ends
  *     each entry point with cudaStreamSynchronize).  Pointers are device
- *     pointers on the current device.  Inputs are borrowed.
+ *     pointers on the current device (host pointers where a call says so).
+ *     Inputs are borrowed.
  *   - y (or C) is OVERWRITTEN; it need not be zeroed first (the reference's
  *     atomic schedules require a zeroed y; overwriting a zeroed y gives the
  *     same result).
@@ -119,9 +128,9 @@ typedef struct el_csr {
  * el_spmv_opts_default. */
 typedef struct el_spmv_opts {
   int32_t threads_per_block; /* thread/group_mapped block size */
-  int32_t items_per_thread;  /* merge_path: merge items per thread and tile
-                                (1..16, tile = 256 x this); work_oriented:
-                                unused (even share per thread) */
+  int32_t items_per_thread;  /* merge_path variants 1 and 2: merge items per
+                                thread and tile (1..16, tile = 256 x this);
+                                variant 0 and work_oriented: unused */
   int32_t threads_per_row;   /* thread_mapped: 1,2,4,8,16,32 lanes per row */
   int32_t group_rows;        /* group_mapped: rows per group: 32 (one warp
                                 per group, the reference's warp_mapped) or
