@@ -80,6 +80,21 @@ class ElSpmvOpts(C.Structure):
     ]
 
 
+class ElEdgePartition(C.Structure):
+    _fields_ = [
+        ("nnz", C.c_int64),
+        ("num_atoms", C.c_int64),
+        ("num_tiles", C.c_int64),
+        ("atoms_x", C.c_int64),
+        ("atoms_y", C.c_int64),
+        ("quarks", C.c_void_p),
+        ("atom_begin", C.c_void_p),
+        ("atom_x", C.c_void_p),
+        ("atom_y", C.c_void_p),
+        ("tile_begin", C.c_void_p),
+    ]
+
+
 class ElBatchItem(C.Structure):
     _fields_ = [("A", ElCsr), ("x", C.c_void_p), ("y", C.c_void_p)]
 
@@ -144,6 +159,21 @@ SIGNATURES = {
     "el_coo_free": (None, [C.POINTER(ElCoo)]),
     "el_csr_from_coo": (C.c_int, [C.c_void_p, C.POINTER(ElCoo), C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p]),
+    "el_coo_sort": (C.c_int, [C.c_void_p, C.POINTER(ElCoo), C.c_int32, C.c_void_p]),
+    "el_csr_row_indices": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p,
+                                     C.c_void_p]),
+    "el_edge_partition_coordinate_plan": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, C.c_int64,
+                                                    C.c_int64, C.c_int64, C.c_int64,
+                                                    C.POINTER(ElEdgePartition)]),
+    "el_edge_partition_position_plan": (C.c_int, [C.c_int64, C.c_int64, C.c_int64,
+                                                  C.POINTER(ElEdgePartition)]),
+    "el_edge_partition_coordinate": (C.c_int, [C.c_void_p, C.POINTER(ElCoo), C.c_int64,
+                                               C.c_int64, C.c_int64, C.c_int64,
+                                               C.POINTER(ElEdgePartition), C.c_void_p]),
+    "el_edge_partition_position": (C.c_int, [C.c_int64, C.c_int64, C.POINTER(ElEdgePartition),
+                                             C.c_void_p]),
+    "el_spmv_edge": (C.c_int, [C.c_void_p, C.POINTER(ElCoo), C.POINTER(ElEdgePartition),
+                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 EL_STATIC_MAX_RANGES = 4096

@@ -31,6 +31,13 @@
  *   el_read_matrix_market / el_csr_from_coo
  *       matrix_market_t::load and csr_t(coo_t)
  *       [include/loops/container/market.hxx:99-227, csr.hxx:86-94]
+ *   el_coo_sort / el_csr_row_indices
+ *       coo_t::sort_by_row, sort_by_column and coo_t(csr_t)
+ *       [include/loops/container/coo.hxx:90-122]
+ *   el_edge_partition_* / el_spmv_edge
+ *       Partitioner and the thread-mapped edge schedule
+ *       [include/loops/util/partitioner.hxx:68-301,
+ *        include/loops/schedule_edge/thread_mapped.hxx:45-117]
  * and adds entry points the reference does not have: el_spmv_host (matrix,
  * x and y in host memory, streamed), el_spmv_static_scratch (no device
  * allocation), the batched plan (el_batch_plan_*), el_quantize_values and
@@ -234,6 +241,89 @@ void el_coo_free(el_coo* coo);
  * `stream` once); the rest is asynchronous. */
 el_status el_csr_from_coo(el_workspace* ws, const el_coo* coo, int32_t* offsets,
                           int32_t* indices, float* values, el_stream_t stream);
+
+/* Sorts a COO whose arrays are in device memory, in place, by (row, column)
+ * (by_column = 0) or (column, row) (by_column = 1), stable.  Replaces
+ * coo_t::sort_by_row / sort_by_column
+ * (include/loops/container/coo.hxx:104-122).  An entry outside the matrix
+ * gives EL_ERR_MALFORMED_CSR before anything is written (synchronises
+ * `stream` once). */
+el_status el_coo_sort(el_workspace* ws, el_coo* coo, int32_t by_column,
+                      el_stream_t stream);
+
+/* The row index of every nonzero of a CSR (nnz entries, device memory):
+ * the row indices of coo_t(csr_t) (include/loops/container/coo.hxx:90-97),
+ * whose column indices and values are the CSR's own arrays. */
+el_status el_csr_row_indices(const int32_t* offsets, int64_t rows, int64_t nnz,
+                             int32_t* row_indices, el_stream_t stream);
+
+/* ---- edge (nonzero) partitioner -----------------------------------------
+ * The reference's Partitioner (include/loops/util/partitioner.hxx:68-301)
+ * and the SpMV over its tiles (schedule_edge/thread_mapped.hxx,
+ * examples/spmv/thread_mapped_edge.cu).  A quark is one nonzero (its
+ * position in the COO), an atom a set of quarks, a tile a set of atoms.
+ *
+ *   coordinate space: atom (ax, ay) = the nonzeros of rows [ax M0, ax M0 +
+ *     M0) and columns [ay K0, ay K0 + K0) in COO order; atoms row-major over
+ *     the atoms_x x atoms_y grid; tile (tx, ty) = atom rows [tx M1, ..) and
+ *     atom columns [ty K1, ..), tiles row-major, atoms in atom order.
+ *   position space: atom i = quarks [i P, i P + P), tile t = atoms
+ *     [t T, t T + T) (the last ones shorter).
+ *
+ * The partition is held as CSR-like arrays in device memory that the caller
+ * allocates from the counts the *_plan call fills in:
+ *   quarks[nnz]                 the quarks, tile by tile, atom by atom;
+ *   atom_begin[num_atoms + 1]   atom a (in tile order) = quarks
+ *                               [atom_begin[a], atom_begin[a + 1]);
+ *   atom_x, atom_y[num_atoms]   the atom's grid coordinates (the
+ *                               reference's x_idx / y_idx; 0 in position
+ *                               space);
+ *   tile_begin[num_tiles + 1]   tile t = atoms [tile_begin[t],
+ *                               tile_begin[t + 1]).
+ * A tile's quarks are therefore one contiguous range of `quarks`.  Sort the
+ * COO by row first (el_coo_sort), as the reference's Partitioner does, for
+ * its quark numbering.  The reference's argument rules hold: sizes > 0,
+ * M0 <= rows, K0 <= cols, M1 <= atoms_x, K1 <= atoms_y, 0 < nnz_per_atom
+ * <= nnz; atoms_per_tile must be > 0 (the reference divides by it). */
+typedef struct el_edge_partition {
+  int64_t nnz, num_atoms, num_tiles;
+  int64_t atoms_x, atoms_y; /* the atom grid (coordinate space), else 0 */
+  int32_t* quarks;
+  int32_t* atom_begin;
+  int32_t* atom_x;
+  int32_t* atom_y;
+  int32_t* tile_begin;
+} el_edge_partition;
+
+/* Fill P's counts (the arrays are left alone). */
+el_status el_edge_partition_coordinate_plan(int64_t rows, int64_t cols,
+                                            int64_t nnz, int64_t M0, int64_t K0,
+                                            int64_t M1, int64_t K1,
+                                            el_edge_partition* P);
+el_status el_edge_partition_position_plan(int64_t nnz, int64_t nnz_per_atom,
+                                          int64_t atoms_per_tile,
+                                          el_edge_partition* P);
+/* Fill P's arrays; P's counts must be the plan's for these arguments.  The
+ * coordinate partition checks every entry is inside the matrix first
+ * (EL_ERR_MALFORMED_CSR; synchronises `stream` once) and uses the
+ * workspace's staging memory; the position partition is asynchronous. */
+el_status el_edge_partition_coordinate(el_workspace* ws, const el_coo* A,
+                                       int64_t M0, int64_t K0, int64_t M1,
+                                       int64_t K1, el_edge_partition* P,
+                                       el_stream_t stream);
+el_status el_edge_partition_position(int64_t nnz_per_atom,
+                                     int64_t atoms_per_tile,
+                                     el_edge_partition* P, el_stream_t stream);
+/* y = A x over the tiles of P, a warp per tile (the reference runs a thread
+ * per tile); FP32, y overwritten, partial sums added atomically so the
+ * summation order varies from run to run.  With quark_tile != NULL,
+ * quark_tile[q] = the tile that processed quark q (the reference's Tracker
+ * records the thread, which is the tile under its one-thread-per-tile
+ * launch).  Quarks, rows or columns outside the arrays are skipped and
+ * raise EL_FLAG_INDEX_RANGE in the workspace's flags (el_workspace_errors). */
+el_status el_spmv_edge(el_workspace* ws, const el_coo* A,
+                       const el_edge_partition* P, const float* x, float* y,
+                       int32_t* quark_tile, el_stream_t stream);
 
 /* C = A B.  B is row-major A->cols x n (leading dimension ldb >= n) of
  * b_dtype (FP32 / BF16 / FP16); C is row-major FP32 A->rows x n (ldc >= n).

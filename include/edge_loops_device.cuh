@@ -18,7 +18,10 @@
 //     calls on_nonzero(row, nz) for every nonzero and on_row_end(row) for
 //     every row that ends inside the range (after that row's nonzeros);
 //   * for_each_row        -- the thread-mapped loop: rows strided over the
-//     grid, on_nonzero(row, nz) then on_row_end(row) per row.
+//     grid, on_nonzero(row, nz) then on_row_end(row) per row;
+//   * edge_tiles / for_each_tile_quark -- the tiles of an edge partition
+//     (quarks grouped into atoms and tiles, edge_loops.h) walked a tile per
+//     thread, the reference's schedule_edge thread_mapped setup.
 //
 // A row that crosses ranges gets on_nonzero calls from several threads and
 // on_row_end from the thread whose range contains its end; combining the
@@ -121,6 +124,36 @@ __device__ __forceinline__ void for_each_row(const int* offsets, int rows, OnNon
     for (int nz = b; nz < e; ++nz) on_nonzero((int)r, nz);
     on_row_end((int)r);
   }
+}
+
+// ---- edge partitions ----------------------------------------------------
+// The tiles of an edge partition (el_edge_partition of edge_loops.h, built
+// by el_edge_partition_coordinate / _position), for user kernels: the
+// reference's schedule_edge::setup<thread_mapped>
+// (schedule_edge/thread_mapped.hxx:45-117), whose tiles() / atoms(tile) /
+// quarks(atom) ranges are index ranges into the partition's arrays here.
+struct edge_tiles {
+  const int* quarks;      // nnz: COO positions, tile by tile, atom by atom
+  const int* atom_begin;  // atoms + 1
+  const int* tile_begin;  // tiles + 1
+  long long num_tiles;
+
+  __device__ int atoms_begin(long long tile) const { return tile_begin[tile]; }
+  __device__ int atoms_end(long long tile) const { return tile_begin[tile + 1]; }
+  __device__ int quarks_begin(int atom) const { return atom_begin[atom]; }
+  __device__ int quarks_end(int atom) const { return atom_begin[atom + 1]; }
+};
+
+// The thread-mapped tile loop: each thread of the grid takes tiles tid,
+// tid + grid size, ... and calls on_quark(tile, atom, q) for every quark q
+// (a COO position) of every atom of the tile, in partition order.
+template <typename OnQuark>
+__device__ __forceinline__ void for_each_tile_quark(const edge_tiles& P, OnQuark on_quark) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < P.num_tiles;
+       t += stride)
+    for (int a = P.atoms_begin(t); a < P.atoms_end(t); ++a)
+      for (int i = P.quarks_begin(a); i < P.quarks_end(a); ++i) on_quark(t, a, P.quarks[i]);
 }
 
 }  // namespace device

@@ -13,7 +13,7 @@ __all__ = [
     "build", "spmv_f32", "spmv_f32_mt", "spmv_f64", "spmm_f32", "spmm_f64", "mp_search",
     "merge_path_tile_coords", "merge_path_thread_coords", "merge_path_walk",
     "work_oriented_coords", "group_mapped_map", "error_metrics", "matrix_market_coo",
-    "csr_from_coo",
+    "csr_from_coo", "coo_sort", "edge_partition_coordinate", "edge_partition_position",
 ]
 
 
@@ -233,3 +233,76 @@ def csr_from_coo(rows, row_indices, col_indices, values):
     order = np.lexsort((ci, ri))  # stable
     offsets = np.searchsorted(ri[order], np.arange(rows + 1), side="left").astype(np.int32)
     return offsets, ci[order].astype(np.int32), np.asarray(values, dtype=np.float32)[order]
+
+
+def coo_sort(row_indices, col_indices, values, by_column=False):
+    """coo_t::sort_by_row / sort_by_column restated (container/coo.hxx:
+    104-122): entries ordered by (row, column) or (column, row); stable, so
+    equal entries keep their order."""
+    ri = np.asarray(row_indices, dtype=np.int64)
+    ci = np.asarray(col_indices, dtype=np.int64)
+    order = np.lexsort((ri, ci)) if by_column else np.lexsort((ci, ri))
+    return (ri[order].astype(np.int32), ci[order].astype(np.int32),
+            np.asarray(values, dtype=np.float32)[order])
+
+
+def _edge_layout(atom_quarks, atom_xy, tile_atoms):
+    """The host-side WorkAtom / WorkTile structure flattened: quarks tile by
+    tile, atom by atom; atom_begin (atoms in tile order); atom_x, atom_y;
+    tile_begin."""
+    quarks, atom_begin, ax, ay, tile_begin = [], [0], [], [], [0]
+    for atoms in tile_atoms:
+        for a in atoms:
+            quarks.extend(atom_quarks[a])
+            atom_begin.append(len(quarks))
+            ax.append(atom_xy[a][0])
+            ay.append(atom_xy[a][1])
+        tile_begin.append(len(ax))
+    i32 = lambda v: np.array(v, dtype=np.int32)  # noqa: E731
+    return {"quarks": i32(quarks), "atom_begin": i32(atom_begin), "atom_x": i32(ax),
+            "atom_y": i32(ay), "tile_begin": i32(tile_begin)}
+
+
+def edge_partition_coordinate(rows, cols, row_indices, col_indices, M0, K0, M1, K1):
+    """The reference's coordinate-space partition restated
+    (util/partitioner.hxx:81-176) over a COO already sorted by row: atom of
+    quark q = (row / M0) * atoms_y + col / K0, the quarks of each atom in q
+    order (:103-117); atom a at (a / atoms_y, a % atoms_y) (:120-124); tile of
+    atom = (x / M1) * tiles_y + y / K1 (:152-157), the atoms of each tile in
+    atom order (:159-173).  Plain loops: small inputs only.  Raises
+    ValueError on the reference's argument errors (:85-93, :133-143)."""
+    if M0 <= 0 or K0 <= 0 or M0 > rows or K0 > cols:
+        raise ValueError("bad atom size")
+    nax, nay = (rows + M0 - 1) // M0, (cols + K0 - 1) // K0
+    if M1 <= 0 or K1 <= 0 or M1 > nax or K1 > nay:
+        raise ValueError("bad tile size")
+    ntx, nty = (nax + M1 - 1) // M1, (nay + K1 - 1) // K1
+    atom_quarks = [[] for _ in range(nax * nay)]
+    for q, (r, c) in enumerate(zip(np.asarray(row_indices).tolist(),
+                                   np.asarray(col_indices).tolist())):
+        atom_quarks[(r // M0) * nay + c // K0].append(q)
+    atom_xy = [(a // nay, a % nay) for a in range(nax * nay)]
+    tile_atoms = [[] for _ in range(ntx * nty)]
+    for a, (x, y) in enumerate(atom_xy):
+        tile_atoms[(x // M1) * nty + y // K1].append(a)
+    out = _edge_layout(atom_quarks, atom_xy, tile_atoms)
+    out["atoms_x"], out["atoms_y"] = nax, nay
+    return out
+
+
+def edge_partition_position(nnz, nnz_per_atom, atoms_per_tile):
+    """The reference's position-space partition restated
+    (util/partitioner.hxx:178-226): atom i = quarks [i P, min(i P + P,
+    nnz)) with coordinates (0, 0); tile t = atoms [t T, min(t T + T,
+    atoms))."""
+    if nnz_per_atom <= 0 or nnz_per_atom > nnz or atoms_per_tile <= 0:
+        raise ValueError("bad atom or tile size")
+    atoms = (nnz + nnz_per_atom - 1) // nnz_per_atom
+    tiles = (atoms + atoms_per_tile - 1) // atoms_per_tile
+    atom_quarks = [list(range(i * nnz_per_atom, min(i * nnz_per_atom + nnz_per_atom, nnz)))
+                   for i in range(atoms)]
+    tile_atoms = [list(range(t * atoms_per_tile, min(t * atoms_per_tile + atoms_per_tile,
+                                                     atoms))) for t in range(tiles)]
+    out = _edge_layout(atom_quarks, [(0, 0)] * atoms, tile_atoms)
+    out["atoms_x"], out["atoms_y"] = 0, 0
+    return out
