@@ -729,6 +729,71 @@ def run_csr_build(args):
     }
 
 
+def run_edge(args):
+    """y = A x over an edge partition (el_spmv_edge) of the power-law
+    matrix's COO: --edge pos:P:T (atoms of P nonzeros, tiles of T atoms) or
+    coord:M0:K0:M1:K1.  Bytes per step: quark, row, column and value per
+    nonzero (16 B), x and y once.  Checked against FP64 within the FP32
+    order-free bound; the partition build is timed once beside it."""
+    import numpy as np
+    import torch
+    import oracle
+    from edge_loops_gb300 import api, edge, synth
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    off, idx, vals, x, cols = synth.power_law(rows=1 << 20, target_nnz=16_000_000, exponent=2.0,
+                                              cap=100_000, seed=1, device=dev)
+    A = api.CSR(off, idx, vals, off.numel() - 1, cols)
+    coo = edge.COO.from_csr(A)
+    spec = args.edge.split(":")
+    sizes = [int(v) for v in spec[1:]]
+    part = edge.Partitioner(coo, sort=False)  # already row-sorted
+    ws = api.Workspace()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, device=dev)
+
+    def build():
+        if spec[0] == "coord":
+            part.partition_atoms_coordinate_space(*sizes[:2])
+            part.partition_tiles_coordinate_space(*sizes[2:])
+        else:
+            part.partition_atoms_position_space(sizes[0])
+            part.partition_tiles_position_space(sizes[1])
+    build_ms = _time_device(build, 3, 3, flush, torch.cuda.current_stream())
+    y = torch.empty(A.rows, device=dev)
+    ms = _time_device(lambda: edge.spmv_edge(coo, part, x, y, workspace=ws), args.steps,
+                      args.warmup, flush, torch.cuda.current_stream())
+    flags = api.workspace_errors(ws)
+    o, i, v, xh = (t.cpu().numpy() for t in (off, idx, vals, x))
+    y64, yabs = oracle.spmv_f64(o, i, v, xh)
+    lens = np.diff(o).astype(np.float64)
+    bound = (lens + 8) * 2.0 ** -24 / (1 - (lens + 8) * 2.0 ** -24) * yabs
+    ok = flags == 0 and bool(np.all(np.abs(y.cpu().numpy().astype(np.float64) - y64) <= bound))
+    if not ok:
+        raise SystemExit("el_spmv_edge outside the FP32 bound of the FP64 oracle")
+    comp, _ = oracle.error_metrics(y.cpu().numpy(), y64, yabs)
+    rows, nnz = A.rows, A.nnz
+    nbytes = nnz * 16 + 4 * cols + 4 * rows
+    import time as _t
+    t0 = _t.perf_counter()
+    oracle.spmv_f32(o, i, v, xh)
+    cpu_s = _t.perf_counter() - t0
+    return {
+        "metric": "edge-partitioned SpMV bandwidth (COO + quarks read, x, y / time)",
+        "value": round(nbytes / (ms * 1e-3) / 1e9, 2), "unit": "GB/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (the 2^20 x 2^20 power-law matrix, seed 1, as a row-sorted COO)",
+        "config": {"workload": "edge SpMV, power-law 2^20 x 2^20, %d nnz" % nnz,
+                   "partition": args.edge, "tiles": part.get_num_tiles(),
+                   "partition_build_ms": round(build_ms, 4), "bytes_per_step": nbytes,
+                   "l2": "flushed between steps"},
+        "check": {"within_fp32_bound_of_fp64": ok, "max_rel_err": comp},
+        "cpu_baseline": {"value": round(nbytes / cpu_s / 1e9, 3), "unit": "GB/s", "cores": 1,
+                         "kind": "port", "sample": "the reference's CPU SpMV loop on the CSR, once"},
+        "gpu_launches": args.steps,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -749,6 +814,8 @@ def main():
     ap.add_argument("--n", type=int, default=128, help="SpMM: columns of B")
     ap.add_argument("--b-dtype", default="f32", choices=["f32", "bf16", "f16"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--edge", default="pos:256:1",
+                    help="spmv_edge partition: pos:P:T or coord:M0:K0:M1:K1")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -769,9 +836,9 @@ def main():
     if world > 1:
         torch.distributed.init_process_group(
             "nccl", device_id=torch.device("cuda", _env_int("LOCAL_RANK", 0)))
-    if args.workload in ("spmm_powerlaw", "spmv_batched", "csr_build"):
+    if args.workload in ("spmm_powerlaw", "spmv_batched", "csr_build", "spmv_edge"):
         line = {"spmm_powerlaw": run_spmm, "spmv_batched": run_batched,
-                "csr_build": run_csr_build}[args.workload](args)
+                "csr_build": run_csr_build, "spmv_edge": run_edge}[args.workload](args)
         if rank == 0:
             print(json.dumps(line))
         return

@@ -211,6 +211,7 @@ __global__ void __launch_bounds__(256)
                      const int32_t* __restrict__ tile_begin, long long tiles,
                      int32_t* __restrict__ quark_tile, unsigned* __restrict__ flags) {
   constexpr unsigned kFull = 0xffffffffu;
+  constexpr int kChunks = 4;
   const int lane = threadIdx.x & 31;
   const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
   bool bad = false;
@@ -218,36 +219,53 @@ __global__ void __launch_bounds__(256)
        t += warps) {
     const long long a0 = min(max((long long)tile_begin[t], 0LL), atoms);
     const long long a1 = min(max((long long)tile_begin[t + 1], a0), atoms);
-    const int qb = (int)min(max((long long)atom_begin[a0], 0LL), nnz);
-    const int qe = (int)min(max((long long)atom_begin[a1], (long long)qb), nnz);
-    for (int base = qb; base < qe; base += 32) {
-      const int i = base + lane;
-      bool ok = i < qe;
-      int r = -1;
-      float p = 0.f;
-      if (ok) {
-        const int q = quarks[i];
-        ok = (unsigned long long)(unsigned)q < (unsigned long long)nnz;
-        const int rr = ok ? ri[q] : 0, c = ok ? ci[q] : 0;
-        ok = ok && (unsigned long long)(unsigned)rr < (unsigned long long)rows &&
-             (unsigned long long)(unsigned)c < (unsigned long long)cols;
-        bad |= i < qe && !ok;
-        if (ok) {
-          r = rr;
-          p = __fmul_rn(val[q], __ldg(x + c));
-          if (quark_tile) quark_tile[q] = (int32_t)t;
-        }
-      }
-      const int rp = __shfl_up_sync(kFull, r, 1);
-      const unsigned heads = __ballot_sync(kFull, lane == 0 || rp != r);
-      const int start = 31 - __clz(heads & (kFull >> (31 - lane)));  // this run's first lane
+    const long long qb = min(max((long long)atom_begin[a0], 0LL), nnz);
+    const long long qe = min(max((long long)atom_begin[a1], qb), nnz);
+    // four 32-quark chunks per step, their loads issued together
+    for (long long base = qb; base < qe; base += 32 * kChunks) {
+      int q[kChunks], r[kChunks], c[kChunks];
+      bool ok[kChunks];
+      float v[kChunks], p[kChunks];
 #pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        const float o = __shfl_up_sync(kFull, p, d);
-        if (lane - d >= start) p += o;
+      for (int k = 0; k < kChunks; ++k) {
+        const long long i = base + 32 * k + lane;
+        ok[k] = i < qe;
+        q[k] = ok[k] ? quarks[i] : 0;
+        const bool in = (unsigned long long)(unsigned)q[k] < (unsigned long long)nnz;
+        bad |= ok[k] && !in;
+        ok[k] = ok[k] && in;
       }
-      const int rn = __shfl_down_sync(kFull, r, 1);
-      if (ok && (lane == 31 || rn != r)) atomicAdd(y + r, p);
+#pragma unroll
+      for (int k = 0; k < kChunks; ++k) {
+        r[k] = ok[k] ? ri[q[k]] : 0;
+        c[k] = ok[k] ? ci[q[k]] : 0;
+        v[k] = ok[k] ? val[q[k]] : 0.f;
+      }
+#pragma unroll
+      for (int k = 0; k < kChunks; ++k) {
+        const bool in = (unsigned long long)(unsigned)r[k] < (unsigned long long)rows &&
+                        (unsigned long long)(unsigned)c[k] < (unsigned long long)cols;
+        bad |= ok[k] && !in;
+        ok[k] = ok[k] && in;
+        p[k] = ok[k] ? __fmul_rn(v[k], __ldg(x + c[k])) : 0.f;
+        if (!ok[k]) r[k] = -1;
+        if (ok[k] && quark_tile) quark_tile[q[k]] = (int32_t)t;
+      }
+#pragma unroll
+      for (int k = 0; k < kChunks; ++k) {
+        if (base + 32 * k >= qe) break;  // warp-uniform
+        const int rp = __shfl_up_sync(kFull, r[k], 1);
+        const unsigned heads = __ballot_sync(kFull, lane == 0 || rp != r[k]);
+        const int start = 31 - __clz(heads & (kFull >> (31 - lane)));  // the run's first lane
+        float s = p[k];
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const float o = __shfl_up_sync(kFull, s, d);
+          if (lane - d >= start) s += o;
+        }
+        const int rn = __shfl_down_sync(kFull, r[k], 1);
+        if (ok[k] && (lane == 31 || rn != r[k])) atomicAdd(y + r[k], s);
+      }
     }
   }
   if (bad) atomicOr(flags, EL_FLAG_INDEX_RANGE);
