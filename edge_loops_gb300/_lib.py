@@ -95,6 +95,15 @@ class ElEdgePartition(C.Structure):
     ]
 
 
+class ElRowStats(C.Structure):
+    _fields_ = [
+        ("max_row_nnz", C.c_int64),
+        ("empty_rows", C.c_int64),
+        ("mean_row_nnz", C.c_double),
+        ("cv", C.c_double),
+    ]
+
+
 class ElBatchItem(C.Structure):
     _fields_ = [("A", ElCsr), ("x", C.c_void_p), ("y", C.c_void_p)]
 
@@ -172,6 +181,13 @@ SIGNATURES = {
                                                C.POINTER(ElEdgePartition), C.c_void_p]),
     "el_edge_partition_position": (C.c_int, [C.c_int64, C.c_int64, C.POINTER(ElEdgePartition),
                                              C.c_void_p]),
+    "el_csr_row_stats": (C.c_int, [C.c_void_p, C.POINTER(ElCsr), C.POINTER(ElRowStats),
+                                   C.c_void_p]),
+    "el_select_schedule": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, C.c_int64,
+                                     C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_double)]),
+    "el_spmv_select": (C.c_int, [C.c_void_p, C.POINTER(ElCsr), C.POINTER(C.c_int32),
+                                 C.POINTER(ElSpmvOpts), C.c_void_p]),
     "el_spmv_edge": (C.c_int, [C.c_void_p, C.POINTER(ElCoo), C.POINTER(ElEdgePartition),
                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 }

@@ -181,6 +181,30 @@ def spmv(A, x, y=None, schedule="merge_path_flat", stream=None, workspace=None, 
     return y
 
 
+def row_stats(A, stream=None, workspace=None):
+    """el_csr_row_stats: longest row, empty rows, mean row length and its
+    coefficient of variation (synchronises the stream)."""
+    st = L.ElRowStats()
+    a = A.el()
+    L.check(L.lib().el_csr_row_stats(_ws(workspace), C.byref(a), C.byref(st), _stream(stream)),
+            "el_csr_row_stats")
+    return {"max_row_nnz": int(st.max_row_nnz), "empty_rows": int(st.empty_rows),
+            "mean_row_nnz": float(st.mean_row_nnz), "cv": float(st.cv)}
+
+
+def select_schedule(A, stream=None, workspace=None):
+    """el_spmv_select: (schedule name, options) for spmv(A, x, schedule=...,
+    **options), chosen once from A's row statistics by the cost model."""
+    sched = C.c_int32(0)
+    o = make_opts()
+    a = A.el()
+    L.check(L.lib().el_spmv_select(_ws(workspace), C.byref(a), C.byref(sched), C.byref(o),
+                                   _stream(stream)), "el_spmv_select")
+    if sched.value == L.EL_SCHED_THREAD_MAPPED:
+        return "thread_mapped", {"threads_per_row": int(o.threads_per_row)}
+    return "merge_path_flat", {}
+
+
 def spmv_host(A, x, y=None, schedule="merge_path_flat", block_nnz=0, stream=None,
               workspace=None, **opts):
     """el_spmv_host: y = A x with A (CSR of CPU tensors), x and y in host

@@ -359,7 +359,16 @@ el_status el_spmv(el_workspace* ws, const el_csr* A, int32_t schedule,
   el_workspace* w = nullptr;
   s = resolve_ws(ws, c.stream, c.device, &w);
   if (s != EL_OK) return s;
-  if (schedule == EL_SCHED_AUTO) schedule = EL_SCHED_MERGE_PATH_FLAT;
+  if (schedule == EL_SCHED_AUTO) {
+    // the selection cost model with the longest row assumed to hold every
+    // nonzero (nothing else is known without a synchronisation): merge_path
+    // unless the matrix is so small that even then thread_mapped is faster
+    int32_t sched = EL_SCHED_MERGE_PATH_FLAT, tpr = 0;
+    s = el_select_schedule(A->rows, A->cols, A->nnz, A->nnz, &sched, &tpr, nullptr);
+    if (s != EL_OK) return s;
+    schedule = sched;
+    if (schedule == EL_SCHED_THREAD_MAPPED) c.o.threads_per_row = tpr;
+  }
   switch (schedule) {
     case EL_SCHED_MERGE_PATH_FLAT: {
       c.ws = ws_view(w);

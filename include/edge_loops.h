@@ -40,8 +40,9 @@
  *        include/loops/schedule_edge/thread_mapped.hxx:45-117]
  * and adds entry points the reference does not have: el_spmv_host (matrix,
  * x and y in host memory, streamed), el_spmv_static_scratch (no device
- * allocation), the batched plan (el_batch_plan_*), el_quantize_values and
- * el_csr_validate.  include/edge_loops_device.cuh holds the device-side
+ * allocation), the batched plan (el_batch_plan_*), schedule selection
+ * (el_spmv_select, el_select_schedule, el_csr_row_stats),
+ * el_quantize_values and el_csr_validate.  include/edge_loops_device.cuh holds the device-side
  * load-balanced loop API for user kernels (the reference's schedule::setup).
  *
  * Conventions (differences from the reference are deliberate and listed):
@@ -105,7 +106,9 @@ typedef enum el_schedule {
   EL_SCHED_GROUP_MAPPED = 3,
   EL_SCHED_BUCKETING = 4, /* declared by the reference, never implemented:
                              returns EL_ERR_UNSUPPORTED */
-  EL_SCHED_AUTO = 5       /* new: pick by the built-in heuristic */
+  EL_SCHED_AUTO = 5       /* new: the selection model without row
+                             statistics (merge_path but for tiny inputs);
+                             el_spmv_select picks with them */
 } el_schedule;
 
 /* Device error flags (bit set), reported by el_workspace_errors and
@@ -324,6 +327,38 @@ el_status el_edge_partition_position(int64_t nnz_per_atom,
 el_status el_spmv_edge(el_workspace* ws, const el_coo* A,
                        const el_edge_partition* P, const float* x, float* y,
                        int32_t* quark_tile, el_stream_t stream);
+
+/* ---- schedule selection ------------------------------------------------
+ * The predictor the reference's paper fits to its per-matrix timings
+ * (plots/data/heuristics.csv), here a cost model of this library's kernels
+ * on GB300: estimated times of merge_path and of thread_mapped with 1, 4
+ * and 32 lanes per row from (rows, nnz, longest row).  EL_SCHED_AUTO in
+ * el_spmv cannot see the longest row without a synchronisation, so it
+ * applies the model with the longest row taken as nnz (the worst case):
+ * merge_path, the choice that is never far off, except for matrices of a
+ * few hundred nonzeros; callers that multiply by the same matrix
+ * repeatedly call el_spmv_select once and reuse its choice (no cost per
+ * call). */
+typedef struct el_row_stats {
+  int64_t max_row_nnz;
+  int64_t empty_rows;
+  double mean_row_nnz;
+  double cv; /* standard deviation / mean of the row lengths */
+} el_row_stats;
+
+/* Row statistics of A's offsets (one kernel; synchronises `stream`). */
+el_status el_csr_row_stats(el_workspace* ws, const el_csr* A, el_row_stats* out,
+                           el_stream_t stream);
+/* The cost model: schedule (EL_SCHED_MERGE_PATH_FLAT or
+ * EL_SCHED_THREAD_MAPPED), lanes per row for thread_mapped (else 0), and
+ * the estimated time in microseconds (may be NULL).  Host only. */
+el_status el_select_schedule(int64_t rows, int64_t cols, int64_t nnz,
+                             int64_t max_row_nnz, int32_t* schedule,
+                             int32_t* threads_per_row, double* est_us);
+/* el_csr_row_stats + el_select_schedule: writes the schedule, and for
+ * thread_mapped opts->threads_per_row (other fields are left alone). */
+el_status el_spmv_select(el_workspace* ws, const el_csr* A, int32_t* schedule,
+                         el_spmv_opts* opts, el_stream_t stream);
 
 /* C = A B.  B is row-major A->cols x n (leading dimension ldb >= n) of
  * b_dtype (FP32 / BF16 / FP16); C is row-major FP32 A->rows x n (ldc >= n).
