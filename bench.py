@@ -450,14 +450,19 @@ def run_reference(args, rank, world):
     the same workload (FP32), one whole-matrix SpMV per step."""
     if rank != 0:
         return None
+    import torch
     import oracle
     from edge_loops_gb300 import synth
     oracle.build()
-    W = make_workload(args.workload, "cpu", "f32")
-    off = W["off"].numpy()
-    idx = W["idx"].numpy()
-    vals = W["vals"].numpy()
-    x = W["x"].numpy()
+    # the same matrix as the device arm: drawn by the same generator on the
+    # GPU when there is one (torch's CPU and CUDA generators differ), then
+    # moved to host memory; the timed loop runs on the host cores only
+    gen_dev = "cuda" if torch.cuda.is_available() else "cpu"
+    W = make_workload(args.workload, gen_dev, "f32")
+    off = W["off"].cpu().numpy()
+    idx = W["idx"].cpu().numpy()
+    vals = W["vals"].cpu().numpy()
+    x = W["x"].cpu().numpy()
     nbytes = synth.algorithmic_bytes(W["rows"], W["cols"], len(idx), 4)
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
@@ -475,6 +480,7 @@ def run_reference(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generator; SuiteSparse not available)",
         "config": {"workload": W["desc"], "schedule": "reference CPU loop (serial per row)",
+                   "generated_on": gen_dev,
                    "rows": W["rows"], "cols": W["cols"], "nnz": int(len(idx)),
                    "value_dtype": "f32", "algorithmic_bytes_per_step": nbytes},
         "cpu_baseline": {
