@@ -486,11 +486,22 @@ __device__ __forceinline__ void run_range(const Args& a, SmemT& S, const int war
 
   // one ticket per CTA (its warps take ranges ticket * warps_per_cta + w):
   // a range only waits on ranges of CTAs that took their ticket earlier and
-  // are therefore running
+  // are therefore running.  Every CTA reads the epoch before its ticket, so
+  // the CTA that takes the launch's last ticket knows that all of them hold
+  // theirs and hands the workspace back for the next launch right away
+  // (ticket to 0, epoch + 1) instead of a completion count at the end.
   __shared__ unsigned s_ticket[2];
   if (threadIdx.x == 0) {
-    s_ticket[0] = atomicAdd(&hdr->ticket, 1u);
-    s_ticket[1] = read_epoch(hdr);
+    const unsigned ep = read_epoch(hdr);
+    __threadfence();
+    const unsigned t = atomicAdd(&hdr->ticket, 1u);
+    if (t == gridDim.x - 1) {
+      __threadfence();
+      atomicExch(&hdr->ticket, 0u);
+      atomicExch(&hdr->epoch, ep + 1u);
+    }
+    s_ticket[0] = t;
+    s_ticket[1] = ep;
   }
   __syncthreads();
   const long long g = (long long)s_ticket[0] * warps_per_cta + (threadIdx.x >> 5);
@@ -592,13 +603,6 @@ __device__ __forceinline__ void run_range(const Args& a, SmemT& S, const int war
     }
   }
 
-  // the last CTA to finish hands the workspace back for the next launch
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned prev = atomicAdd(&hdr->done, 1u);
-    if (prev == gridDim.x - 1) finish_launch(hdr, epoch);
-  }
 }
 
 template <typename VT, bool COMP>
