@@ -61,10 +61,11 @@ struct SpmvImpl {
 
   template <int TPR, bool COMP>
   static el_status tm(const SpmvCall& c) {
+    // one lane group per row, as the reference launches it (the kernel's
+    // grid-stride loop only matters past the grid size limit)
     const int tpb = 256;
     long long grid = (c.A.rows * TPR + tpb - 1) / tpb;
-    const long long cap = (long long)device_info(c.device).sm_count * 32;
-    if (grid > cap) grid = cap;
+    if (grid > 0x7fffffffLL) grid = 0x7fffffffLL;
     if (grid < 1) grid = 1;
     thread_mapped_spmv_kernel<VT, TPR, COMP><<<(unsigned)grid, tpb, 0, c.stream>>>(basic(c));
     return cuda_status(cudaGetLastError(), "thread_mapped launch");

@@ -45,6 +45,64 @@ __device__ __forceinline__ float scaled(const BasicArgs& a, long long row,
   return a.row_scale ? v * __ldg(a.row_scale + row) : v;
 }
 
+// acc += the products of nonzeros b, b + S, b + 2S, ... < e, added in that
+// order (each product rounded, then the sum: no fused multiply-add).  The
+// nonzeros go in batches of W, software-pipelined: a batch's x gathers are
+// in flight together with the next batch's index and value loads.  A column
+// outside [0, cols) contributes 0, loads nothing and sets `bad` (the caller
+// raises the flag once).
+template <typename VT, int S, bool COMP, int W = 8>
+__device__ __forceinline__ void accumulate(const BasicArgs& a, long long b, long long e,
+                                           Acc<COMP>& acc, bool& bad) {
+  if (b >= e) return;
+  const VT* __restrict__ vals = reinterpret_cast<const VT*>(a.values);
+  const unsigned long long cols = (unsigned long long)a.cols;
+  int c[W];
+  float v[W];
+  unsigned in = 0;  // bit k: nonzero nz + k S is inside [b, e)
+  long long nz = b;
+#pragma unroll
+  for (int k = 0; k < W; ++k) {
+    const bool t = nz + k * S < e;
+    in |= (unsigned)t << k;
+    c[k] = t ? __ldg(a.indices + nz + k * S) : 0;
+    v[k] = t ? to_f32(vals[nz + k * S]) : 0.f;
+  }
+  for (;;) {
+    float xv[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      const bool t = (in >> k) & 1u;
+      const bool ok = (unsigned)c[k] < cols;
+      bad |= t && !ok;
+      xv[k] = t && ok ? __ldg(a.x + c[k]) : 0.f;
+      if (!ok) v[k] = 0.f;
+    }
+    const long long nn = nz + W * S;
+    int c2[W];
+    float v2[W];
+    unsigned in2 = 0;
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      const bool t = nn + k * S < e;
+      in2 |= (unsigned)t << k;
+      c2[k] = t ? __ldg(a.indices + nn + k * S) : 0;
+      v2[k] = t ? to_f32(vals[nn + k * S]) : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < W; ++k)
+      if ((in >> k) & 1u) acc.add(__fmul_rn(v[k], xv[k]));
+    if (!in2) break;
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      c[k] = c2[k];
+      v[k] = v2[k];
+    }
+    in = in2;
+    nz = nn;
+  }
+}
+
 // ------------------------------------------------------------ thread_mapped
 // The reference's thread_mapped / original schedule
 // [include/loops/schedule/thread_mapped.hxx:147-160,
@@ -54,7 +112,7 @@ __device__ __forceinline__ float scaled(const BasicArgs& a, long long row,
 // a fixed xor tree).  With TPR == 1 every row is the reference CPU loop's
 // exact sequence of FP32 roundings (no fused multiply-add).
 template <typename VT, int TPR, bool COMP>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 5)
     thread_mapped_spmv_kernel(const BasicArgs a) {
   const int lane = threadIdx.x & 31;
   const int sub = lane % TPR;
@@ -67,7 +125,9 @@ __global__ void __launch_bounds__(256)
     if (row < a.rows) {
       long long b, e;
       row_bounds(a, row, &b, &e);
-      for (long long nz = b + sub; nz < e; nz += TPR) acc.add(product<VT>(a, nz));
+      bool bad = false;
+      accumulate<VT, TPR, COMP, 8>(a, b + sub, e, acc, bad);
+      if (bad) raise_flag(a.hdr, EL_FLAG_INDEX_RANGE, (unsigned)row);
     }
 #pragma unroll
     for (int d = TPR / 2; d > 0; d >>= 1) {
@@ -236,16 +296,36 @@ __global__ void __launch_bounds__(TPB)
   long long ey = lower - ex;
   if (ex > a.rows) ex = a.rows;
 
+  // The thread's nonzeros [sy, ey) are one contiguous run.  With short
+  // rows they stream in software-pipelined batches of kW whatever the row
+  // boundaries, and the ends of rows [sx, ex) come kE at a time into a
+  // shift register, so short rows cost no round trip each.  Rows from ex on
+  // do not end here (ex is the open row, finished by the carry).
+  constexpr int kW = 8, kE = 8;
+  const VT* __restrict__ vals = reinterpret_cast<const VT*>(a.values);
+  const unsigned long long cols = (unsigned long long)a.cols;
   Acc<COMP> run, first_v;
   long long first_row = -1;
-  long long nz = sy;
-  for (long long row = sx; row < ex; ++row) {
-    long long e = __ldg(a.offsets + row + 1);
-    if (e > ey || e < nz) {
-      raise_flag(a.hdr, EL_FLAG_OFFSETS, (unsigned)row);
-      e = e > ey ? ey : nz;
+  bool bad = false, bad_off = false;
+  long long row = sx;
+  int ends[kE];  // ends[j] = end of row `row + j` (INT_MAX from row ex on)
+  int left = 0;  // valid entries of ends
+  int prev_end = (int)sy;
+  auto refill = [&]() {
+#pragma unroll
+    for (int j = 0; j < kE; ++j) {
+      const long long r = row + j;
+      int e = r < ex ? __ldg(a.offsets + r + 1) : 0x7fffffff;
+      if (r < ex && (e > ey || e < prev_end)) {  // malformed offsets: keep them monotone
+        bad_off = true;
+        e = e > ey ? (int)ey : prev_end;
+      }
+      if (r < ex) prev_end = e;
+      ends[j] = e;
     }
-    for (; nz < e; ++nz) run.add(product<VT>(a, nz));
+    left = kE;
+  };
+  auto close_row = [&]() {
     if (first_row < 0) {
       first_row = row;
       first_v = run;
@@ -253,8 +333,101 @@ __global__ void __launch_bounds__(TPB)
       a.y[row] = scaled(a, row, run.value());
     }
     run = Acc<COMP>();
+    ++row;
+#pragma unroll
+    for (int j = 0; j + 1 < kE; ++j) ends[j] = ends[j + 1];
+    if (--left == 0) refill();
+  };
+  // Long rows (every lane of the warp averaging >= 12 nonzeros per row)
+  // walk row by row, each row's nonzeros pipelined, the next row's end
+  // fetched early; otherwise the nonzeros stream across rows as below.
+  const bool rowwise = __all_sync(0xffffffffu, (ey - sy) >= 12 * (ex - sx));
+  if (rowwise) {
+    long long nz = sy;
+    long long e_next = sx < ex ? __ldg(a.offsets + sx + 1) : 0;
+    for (; row < ex; ++row) {
+      long long e = e_next;
+      if (row + 1 < ex) e_next = __ldg(a.offsets + row + 2);
+      if (e > ey || e < nz) {
+        bad_off = true;
+        e = e > ey ? ey : nz;
+      }
+      accumulate<VT, 1, COMP>(a, nz, e, run, bad);
+      nz = e;
+      if (first_row < 0) {
+        first_row = row;
+        first_v = run;
+      } else {
+        a.y[row] = scaled(a, row, run.value());
+      }
+      run = Acc<COMP>();
+    }
+    if (nz < ey) accumulate<VT, 1, COMP>(a, nz, ey, run, bad);
+  } else {
+    refill();
+    while (row < ex && ends[0] <= sy) close_row();  // rows that end before any nonzero
   }
-  for (; nz < ey; ++nz) run.add(product<VT>(a, nz));
+  if (!rowwise && sy < ey) {
+    int c[kW];
+    float v[kW];
+#pragma unroll
+    for (int k = 0; k < kW; ++k) {
+      const bool t = sy + k < ey;
+      c[k] = t ? __ldg(a.indices + sy + k) : 0;
+      v[k] = t ? to_f32(vals[sy + k]) : 0.f;
+    }
+    for (long long base = sy;; base += kW) {
+      float p[kW];
+#pragma unroll
+      for (int k = 0; k < kW; ++k) {
+        const bool t = base + k < ey;
+        const bool ok = (unsigned)c[k] < cols;
+        bad |= t && !ok;
+        p[k] = t && ok ? __fmul_rn(v[k], __ldg(a.x + c[k])) : 0.f;
+      }
+      const long long nb = base + kW;
+#pragma unroll
+      for (int k = 0; k < kW; ++k) {
+        const bool t = nb + k < ey;
+        c[k] = t ? __ldg(a.indices + nb + k) : 0;
+        v[k] = t ? to_f32(vals[nb + k]) : 0.f;
+      }
+      // rows ending in this batch: none, one (its end position by a
+      // predicated select, one close per batch), or several
+      const bool c1 = row < ex && ends[0] <= nb;
+      const bool c2 = c1 && row + 1 < ex && ends[1] <= nb;
+      if (!c2) {
+        const int q = c1 ? (int)(ends[0] - base) - 1 : kW;  // the row ends after nonzero base + q
+        Acc<COMP> closed;
+#pragma unroll
+        for (int k = 0; k < kW; ++k) {
+          if (base + k < ey) run.add(p[k]);
+          if (k == q) {
+            closed = run;
+            run = Acc<COMP>();
+          }
+        }
+        if (c1) {
+          const Acc<COMP> rest = run;
+          run = closed;
+          close_row();
+          run = rest;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < kW; ++k) {
+          if (base + k < ey) {
+            run.add(p[k]);
+            // rows that end right after this nonzero (and empty rows after them)
+            while (row < ex && ends[0] <= base + k + 1) close_row();
+          }
+        }
+      }
+      if (nb >= ey) break;
+    }
+  }
+  if (bad_off) raise_flag(a.hdr, EL_FLAG_OFFSETS, (unsigned)sx);
+  if (bad) raise_flag(a.hdr, EL_FLAG_INDEX_RANGE, (unsigned)sx);
 
   SegVal<COMP> mine, zero, tot;
   mine.f = first_row >= 0;
