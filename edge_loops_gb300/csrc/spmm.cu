@@ -66,8 +66,46 @@ __device__ __forceinline__ void bounds(const Args& a, long long row, long long* 
   *e = hi;
 }
 
+// sum += A[row, b..e) . B[.., col] in nonzero order (each product rounded,
+// then added), W nonzeros' value and B loads issued together and the next
+// W's index loads in flight with them; a column index outside [0, cols)
+// contributes 0 and sets `bad`.
+template <typename VT, typename BT, int W>
+__device__ __forceinline__ float column_sum(const Args& a, const VT* vals, const BT* B,
+                                            long long b, long long e, int col, bool& bad) {
+  float sum = 0.f;
+  if (b >= e) return sum;
+  const unsigned long long cols = (unsigned long long)a.cols;
+  int c[W];
+#pragma unroll
+  for (int k = 0; k < W; ++k) c[k] = b + k < e ? __ldg(a.indices + b + k) : -1;
+  for (long long nz = b;;) {
+    float bv[W], v[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      const bool t = nz + k < e;
+      const bool ok = (unsigned)c[k] < cols;
+      bad |= t && !ok;
+      bv[k] = t && ok ? ld_f32(B + (long long)c[k] * a.ldb + col) : 0.f;
+      v[k] = t && ok ? to_f32(vals[nz + k]) : 0.f;
+    }
+    const long long nn = nz + W;
+#pragma unroll
+    for (int k = 0; k < W; ++k) c[k] = nn + k < e ? __ldg(a.indices + nn + k) : -1;
+#pragma unroll
+    for (int k = 0; k < W; ++k)
+      if (nz + k < e) sum = __fadd_rn(sum, __fmul_rn(v[k], bv[k]));
+    if (nn >= e) break;
+    nz = nn;
+  }
+  return sum;
+}
+
+// A thread's time is its row's length times the number of columns, so the
+// longest row sets the kernel's: sixteen B loads in flight per step, at
+// three CTAs per SM.
 template <typename VT, typename BT>
-__global__ void __launch_bounds__(256) thread_mapped_kernel(const Args a) {
+__global__ void __launch_bounds__(256, 3) thread_mapped_kernel(const Args a) {
   const VT* vals = reinterpret_cast<const VT*>(a.values);
   const BT* B = reinterpret_cast<const BT*>(a.B);
   for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < a.rows;
@@ -75,15 +113,12 @@ __global__ void __launch_bounds__(256) thread_mapped_kernel(const Args a) {
     long long b, e;
     bounds(a, row, &b, &e);
     const float s = a.row_scale ? __ldg(a.row_scale + row) : 1.f;
+    bool bad = false;
     for (int col = 0; col < a.n; ++col) {
-      float sum = 0.f;
-      for (long long nz = b; nz < e; ++nz) {
-        const int c = __ldg(a.indices + nz);
-        if (!col_ok(a, c, nz)) continue;
-        sum = __fadd_rn(sum, __fmul_rn(to_f32(vals[nz]), ld_f32(B + (long long)c * a.ldb + col)));
-      }
+      const float sum = column_sum<VT, BT, 16>(a, vals, B, b, e, col, bad);
       a.C[row * a.ldc + col] = a.row_scale ? sum * s : sum;
     }
+    if (bad) raise_flag(a.hdr, EL_FLAG_INDEX_RANGE, (unsigned)row);
   }
 }
 
@@ -133,11 +168,30 @@ __global__ void __launch_bounds__(256) group_mapped_kernel(const Args a) {
         if (!col_ok(a, mc, base + lane)) mc = -1;
       }
       const int cnt = (int)(e - base < 32 ? e - base : 32);
-#pragma unroll 4
-      for (int j = 0; j < cnt; ++j) {
-        const int col = __shfl_sync(kFullMask, mc, j);
-        const float v = __shfl_sync(kFullMask, mv, j);
-        if (col >= 0) axpy_row<VT, BT, VEC>(a, B, col, v, acc);
+      // eight nonzeros at a time: their B rows are loaded together, then
+      // added in nonzero order
+      for (int j0 = 0; j0 < cnt; j0 += 8) {  // warp-uniform
+        float bv[8][VEC], vv[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int col = __shfl_sync(kFullMask, mc, (j0 + j) & 31);
+          vv[j] = __shfl_sync(kFullMask, mv, (j0 + j) & 31);
+          const bool use = j0 + j < cnt && col >= 0;
+          const BT* brow = B + (long long)(use ? col : 0) * a.ldb;
+#pragma unroll
+          for (int k = 0; k < VEC; ++k) {
+            const int cc = lane + 32 * k;
+            bv[j][k] = use && cc < a.n ? ld_f32(brow + cc) : 0.f;
+          }
+          if (!use) vv[j] = 0.f;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          if (j0 + j < cnt) {
+#pragma unroll
+            for (int k = 0; k < VEC; ++k) acc[k] = __fadd_rn(acc[k], __fmul_rn(vv[j], bv[j][k]));
+          }
+        }
       }
     }
     store_row<VEC>(a, row, acc);

@@ -34,8 +34,9 @@ names = re.findall(r"Compiling entry function '([^']+)'",
 kernels = {}
 for key, tag in (("merge_path_flat", "__merge_path_flat"), ("thread_mapped", "__thread_mapped"),
                  ("group_mapped", "__group_mapped"), ("work_oriented", "__work_oriented"),
-                 ("original", "__original")):
-    hit = [n for n in names if str(len(tag)) + tag in n]
+                 ("original", "__original"), ("spmm_thread_mapped", "__thread_mapped")):
+    pre = "4spmm" if key.startswith("spmm") else "4spmv"
+    hit = [n for n in names if pre + str(len(tag)) + tag in n]
     assert len(hit) == 1, (key, hit)
     kernels[key] = hit[0]
 layout = json.loads(subprocess.check_output([os.path.join(out, "ref_kernels_layout")]))

@@ -16,7 +16,9 @@ reference's launcher does:
   thread_mapped    block 128, one thread per row (thread_mapped.cuh:74-88);
   group_mapped     block 128, ceil(rows / 128) blocks (group_mapped.cuh:79-90);
   work_oriented    block 128, 2 x SMs blocks (work_oriented.cuh:97-108);
-  original         block 128, one thread per row (original.cuh:65-72).
+  original         block 128, one thread per row (original.cuh:65-72);
+  spmm thread_mapped  block 128, one thread per row of C, all columns
+                   (algorithms/spmm/thread_mapped.cuh:67-86).
 
 y is zeroed first (the atomic schedules add into it).  The arrays handed to
 the kernels come from pad(): copies with zeroed room after the end, because
@@ -90,6 +92,37 @@ class RefKernels:
             assert i >= 0 and b.find(pat, i + 1) < 0, key
             b[i:i + 8] = int(val).to_bytes(8, "little")
         return (C.c_ubyte * len(b)).from_buffer_copy(bytes(b))
+
+    def _matrix_bytes(self, rows, cols, ptr):
+        """A dense matrix_t passed by value: the sentinels replaced, the
+        vector member (neither copied nor read on the GPU) zeroed."""
+        t = bytes.fromhex(self.info["matrix"])
+        s = self.info["sentinels"]
+        out = bytearray(len(t))
+        for key, val in (("rows", rows), ("nnz", cols), ("offsets", ptr)):
+            pat = bytes.fromhex(s[key])
+            i = t.find(pat)
+            assert i >= 0 and t.find(pat, i + 1) < 0, key
+            out[i:i + 8] = int(val).to_bytes(8, "little")
+        return (C.c_ubyte * len(out)).from_buffer_copy(bytes(out))
+
+    def spmm(self, rows, cols, nnz, offsets, indices, values, B, Cm):
+        """C = A B by the reference's SpMM kernel on the current stream; B is
+        row-major cols x n and C row-major rows x n (contiguous float32)."""
+        import torch
+        s = torch.cuda.current_stream()
+        n = B.shape[1]
+        u64 = C.c_uint64
+        args = [self._setup_bytes(offsets.data_ptr(), rows, nnz), u64(rows), u64(cols), u64(nnz),
+                C.c_void_p(offsets.data_ptr()), C.c_void_p(indices.data_ptr()),
+                C.c_void_p(values.data_ptr()), self._matrix_bytes(cols, n, B.data_ptr()),
+                self._matrix_bytes(rows, n, Cm.data_ptr())]
+        params = (C.c_void_p * len(args))(*[C.cast(C.pointer(a), C.c_void_p) for a in args])
+        grid = max(-(-rows // 128), 1)
+        self._check(self.cu.cuLaunchKernel(self.fn["spmm_thread_mapped"], grid, 1, 1, 128, 1, 1,
+                                           0, C.c_void_p(s.cuda_stream), params, None),
+                    "cuLaunchKernel spmm_thread_mapped")
+        return Cm
 
     def launch(self, schedule, rows, cols, nnz, offsets, indices, values, x, y, zero=True):
         """One SpMV y = A x by the reference kernel of `schedule` on the

@@ -40,3 +40,30 @@ def test_reference_kernels_agree_with_the_library(cuda, oracle_mod):
         # the library's work_oriented is within the bound everywhere
         mine = api.spmv(A, xd, schedule="work_oriented").cpu().numpy().astype(np.float64)
         assert np.all(np.abs(mine - y64) <= bound)
+
+
+@pytest.mark.gpu
+def test_reference_spmm_agrees_with_the_library(cuda, oracle_mod):
+    import torch
+    from edge_loops_gb300 import api
+    from oracle.ref import ref_gpu
+    if not ref_gpu.available():
+        pytest.skip("oracle/_ref/ref_kernels.cubin not built (needs the reference sources)")
+    R = ref_gpu.RefKernels()
+    rng = np.random.default_rng(67)
+    off, idx, vals, _ = random_csr(rng, rows=3000, cols=2000, max_len=30, empty_frac=0.2,
+                                   long_rows=[(11, 1900)])
+    A = api.CSR.from_arrays(off, idx, vals, 2000, device="cuda")
+    for n in (1, 7, 32):
+        B = torch.from_numpy(rng.uniform(-1, 1, (2000, n)).astype(np.float32)).cuda()
+        P = [ref_gpu.pad(t) for t in (A.offsets, A.indices, A.values)]
+        Cr = torch.empty(A.rows, n, device="cuda")
+        R.spmm(A.rows, A.cols, A.nnz, *P, B, Cr)
+        ref = Cr.cpu().numpy().astype(np.float64)
+        c64, cabs = oracle_mod.spmm_f64(off, idx, vals, B.cpu().numpy())
+        lens = np.diff(off).astype(np.float64)[:, None]
+        bound = (lens + 2) * 2.0 ** -24 / (1 - (lens + 2) * 2.0 ** -24) * cabs
+        assert np.all(np.abs(ref - c64) <= bound), n
+        for sched in ("thread_mapped", "group_mapped", "merge_path_flat"):
+            mine = api.spmm(A, B, schedule=sched).cpu().numpy().astype(np.float64)
+            assert np.all(np.abs(mine - c64) <= bound), (n, sched)
