@@ -109,13 +109,35 @@ __device__ __forceinline__ void rows_tpr(const Desc& d, int r0, int r1, int lane
         b = min(max(b, 0), d.nnz);
         e = min(max(e, b), d.nnz);
       }
-      for (int nz = b + sub; nz < e; nz += TPR) {
-        const int col = __ldg(d.indices + nz);
-        if ((unsigned)col < (unsigned)d.cols)
-          acc = __fadd_rn(acc, __fmul_rn(to_f32(vals[nz]), __ldg(d.x + col)));
-        else
-          raise_flag(hdr, EL_FLAG_INDEX_RANGE, (unsigned)nz);
+      // four nonzeros' index, value and x loads issued together, added in
+      // nonzero order; a bad column adds 0 and raises the flag once
+      bool bad = false;
+      int nz = b + sub;
+      for (; nz + 3 * TPR < e; nz += 4 * TPR) {
+        int c[4];
+        float v[4], xv[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          c[k] = __ldg(d.indices + nz + k * TPR);
+          v[k] = to_f32(vals[nz + k * TPR]);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const bool ok = (unsigned)c[k] < (unsigned)d.cols;
+          bad |= !ok;
+          xv[k] = ok ? __ldg(d.x + c[k]) : 0.f;
+          if (!ok) v[k] = 0.f;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) acc = __fadd_rn(acc, __fmul_rn(v[k], xv[k]));
       }
+      for (; nz < e; nz += TPR) {
+        const int col = __ldg(d.indices + nz);
+        const bool ok = (unsigned)col < (unsigned)d.cols;
+        bad |= !ok;
+        acc = __fadd_rn(acc, ok ? __fmul_rn(to_f32(vals[nz]), __ldg(d.x + col)) : 0.f);
+      }
+      if (bad) raise_flag(hdr, EL_FLAG_INDEX_RANGE, (unsigned)row);
     }
 #pragma unroll
     for (int o = TPR / 2; o > 0; o >>= 1) acc = __fadd_rn(acc, __shfl_xor_sync(kFullMask, acc, o));
