@@ -29,17 +29,6 @@ __device__ __forceinline__ void row_bounds(const BasicArgs& a, long long row,
   *e = hi;
 }
 
-template <typename VT>
-__device__ __forceinline__ float product(const BasicArgs& a, long long nz) {
-  const int col = __ldg(a.indices + nz);
-  if ((unsigned)col >= (unsigned long long)a.cols) {
-    raise_flag(a.hdr, EL_FLAG_INDEX_RANGE, (unsigned)nz);
-    return 0.f;
-  }
-  return __fmul_rn(to_f32(reinterpret_cast<const VT*>(a.values)[nz]),
-                   __ldg(a.x + col));
-}
-
 __device__ __forceinline__ float scaled(const BasicArgs& a, long long row,
                                         float v) {
   return a.row_scale ? v * __ldg(a.row_scale + row) : v;
@@ -190,9 +179,27 @@ __global__ void __launch_bounds__(TPB)
     const long long abeg = glen > 0 ? s_off[grp][0] : 0;
     long long aend = glen > 0 ? s_off[grp][glen] : 0;
     if (aend < abeg) aend = abeg;
-    // group-uniform loop over chunks of GT nonzeros
+    // group-uniform loop over chunks of GT nonzeros; each thread's index
+    // and value for the next chunk load while this chunk's x gathers are
+    // in flight
+    const VT* __restrict__ vals = reinterpret_cast<const VT*>(a.values);
+    bool bad = false;
+    int cn = 0;
+    float vn = 0.f;
+    if (abeg + t < aend) {
+      cn = __ldg(a.indices + abeg + t);
+      vn = to_f32(vals[abeg + t]);
+    }
     for (long long base = abeg; base < aend; base += GT) {
       const long long nz = base + t;
+      const int c = cn;
+      float v = vn;
+      const bool ok = (unsigned)c < (unsigned long long)a.cols;
+      const float xv = nz < aend && ok ? __ldg(a.x + c) : 0.f;
+      if (nz + GT < aend) {
+        cn = __ldg(a.indices + nz + GT);
+        vn = to_f32(vals[nz + GT]);
+      }
       SegVal<COMP> mine;
       int key = GT;  // sentinel for threads past the group's nonzeros
       mine.f = 1;
@@ -207,7 +214,9 @@ __global__ void __launch_bounds__(TPB)
         if (key < 0) key = 0;
         if (key > glen - 1) key = glen - 1;
         mine.f = (t == 0) || (nz == s_off[grp][key]);
-        mine.v.add(product<VT>(a, nz));
+        bad |= !ok;
+        if (!ok) v = 0.f;
+        mine.v.add(__fmul_rn(v, xv));
         tail = (t == GT - 1) || (nz + 1 == aend) || (nz + 1 >= s_off[grp][key + 1]);
       }
       SegVal<COMP> inc;
@@ -229,6 +238,7 @@ __global__ void __launch_bounds__(TPB)
       }
       gsync();
     }
+    if (bad) raise_flag(a.hdr, EL_FLAG_INDEX_RANGE, (unsigned)r0);
     gsync();
     if (t < glen) {
       Acc<COMP> acc;
