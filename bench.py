@@ -779,6 +779,7 @@ def run_edge(args):
     comp, _ = oracle.error_metrics(y.cpu().numpy(), y64, yabs)
     rows, nnz = A.rows, A.nnz
     nbytes = nnz * 16 + 4 * cols + 4 * rows
+    peak, src = measured_peaks()
     import time as _t
     t0 = _t.perf_counter()
     oracle.spmv_f32(o, i, v, xh)
@@ -794,6 +795,10 @@ def run_edge(args):
                    "partition_build_ms": round(build_ms, 4), "bytes_per_step": nbytes,
                    "l2": "flushed between steps"},
         "check": {"within_fp32_bound_of_fp64": ok, "max_rel_err": comp},
+        "roofline": {"bound": "hbm", "achieved": round(nbytes / (ms * 1e-3) / 1e9, 2),
+                     "peak": peak, "unit": "GB/s",
+                     "frac": round(nbytes / (ms * 1e-3) / 1e9 / peak, 4), "peak_source": src,
+                     "traffic": traffic_for(f"spmv_edge:{args.edge}")},
         "cpu_baseline": {"value": round(nbytes / cpu_s / 1e9, 3), "unit": "GB/s", "cores": 1,
                          "kind": "port", "sample": "the reference's CPU SpMV loop on the CSR, once"},
         "gpu_launches": args.steps,
