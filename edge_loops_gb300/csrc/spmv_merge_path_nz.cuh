@@ -221,6 +221,11 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
   int hi = tile_hi(lo);
   load_tile(lo, hi);
   int o = load_ends(ra);
+  // scales of rows ra + lane, fetched with the row-end window they belong to
+  auto load_scales = [&](int r) {
+    return scale && r + lane < rows ? __ldg(scale + r + lane) : 1.f;
+  };
+  float scn = load_scales(ra);
   int o2 = 0;          // ends of the next 32 rows, when the last tile predicts them
   bool has_o2 = false;
   gather();
@@ -255,9 +260,9 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
       }
     }
     const bool fast = __all_sync(kFullMask, rising) && X < kMaxEnds && hi - lo == kTileNz;
-    // row scales of the tile's first 32 rows: loaded now, used by the store
-    // at the end of the tile
-    const float sc0 = scale && lane < X ? __ldg(scale + ra + lane) : 1.f;
+    // row scales of the tile's first 32 rows (fetched with their row-end
+    // window, a tile ahead), used by the store at the end of the tile
+    const float sc0 = scn;
     if (!fast && lane < X) S.re[lane] = el0;
     __syncwarp();
     if (X >= kMaxEnds) hi = lo + S.re[kMaxEnds - 1];  // cut the tile at its 256th row end
@@ -279,7 +284,10 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
     // the window registers are free: start loading the next tile
     const int lo2 = hi, hi2 = tile_hi(hi), ra2 = ra + X;
     if (lo2 < ne) load_tile(lo2, hi2);
-    if (ra2 < re) o = load_ends(ra2);
+    if (ra2 < re) {
+      o = load_ends(ra2);
+      scn = load_scales(ra2);
+    }
     // a tile with many row ends is likely followed by another: fetch the
     // second window too, so that its ballot does not wait on a dependent load
     has_o2 = X >= 24 && ra2 + 32 < re;
