@@ -57,12 +57,12 @@ struct Cost {
   double a, c, d, e;  // a + c max_row + d rows/1e3 + e nnz/1e6 (us)
 };
 // merge_path: a + e (nnz + rows)/1e6 (c = d = 0)
-constexpr Cost kMergePath = {15.35, 0.0, 0.0, 3.962};
+constexpr Cost kMergePath = {14.66, 0.0, 0.0, 3.901};
 constexpr int kTprs[3] = {1, 4, 32};
 constexpr Cost kThreadMapped[3] = {
-    {6.727, 0.1596, 0.0, 6.867},     // one lane per row (the reference's thread_mapped)
-    {6.281, 0.08171, 0.01748, 3.222},
-    {6.493, 0.02623, 0.1337, 2.420},  // a warp per row
+    {7.034, 0.06009, 0.00394, 5.571},  // one lane per row (the reference's thread_mapped)
+    {6.698, 0.04393, 0.02568, 3.156},
+    {6.71, 0.007042, 0.2044, 1.804},   // a warp per row
 };
 
 }  // namespace

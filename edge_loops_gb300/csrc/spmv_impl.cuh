@@ -59,13 +59,17 @@ struct SpmvImpl {
     return a;
   }
 
+  static constexpr long long kTmCtasPerSm = 64;
   template <int TPR, bool COMP>
   static el_status tm(const SpmvCall& c) {
-    // one lane group per row, as the reference launches it (the kernel's
-    // grid-stride loop only matters past the grid size limit)
+    // one lane group per row, up to a cap (opts.max_ctas, else
+    // kTmCtasPerSm CTAs per SM): past it the lane groups stride over rows
     const int tpb = 256;
     long long grid = (c.A.rows * TPR + tpb - 1) / tpb;
-    if (grid > 0x7fffffffLL) grid = 0x7fffffffLL;
+    const long long cap = c.o.max_ctas > 0
+                              ? (long long)c.o.max_ctas
+                              : (long long)device_info(c.device).sm_count * kTmCtasPerSm;
+    if (grid > cap) grid = cap;
     if (grid < 1) grid = 1;
     thread_mapped_spmv_kernel<VT, TPR, COMP><<<(unsigned)grid, tpb, 0, c.stream>>>(basic(c));
     return cuda_status(cudaGetLastError(), "thread_mapped launch");

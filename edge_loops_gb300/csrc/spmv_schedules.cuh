@@ -115,7 +115,18 @@ __global__ void __launch_bounds__(256, 5)
       long long b, e;
       row_bounds(a, row, &b, &e);
       bool bad = false;
-      accumulate<VT, TPR, COMP, 8>(a, b + sub, e, acc, bad);
+      if (TPR == 1) {
+        accumulate<VT, 1, COMP, 8>(a, b, e, acc, bad);
+      } else {
+        // a lane sees few nonzeros of a row: a plain strided loop
+        const VT* __restrict__ vals = reinterpret_cast<const VT*>(a.values);
+        for (long long nz = b + sub; nz < e; nz += TPR) {
+          const int col = __ldg(a.indices + nz);
+          const bool ok = (unsigned)col < (unsigned long long)a.cols;
+          bad |= !ok;
+          acc.add(ok ? __fmul_rn(to_f32(vals[nz]), __ldg(a.x + col)) : 0.f);
+        }
+      }
       if (bad) raise_flag(a.hdr, EL_FLAG_INDEX_RANGE, (unsigned)row);
     }
 #pragma unroll

@@ -4,7 +4,7 @@ nnz, longest row), a schedule whose measured time is close to the best one.
 CPU: the model's choices on the committed GB300 sweep
 (tests/data/select_sweep_gb300.csv, made by edge_loops_gb300/tune_select.py:
 every schedule timed on 119 synthetic shapes) are within 2 % of the best
-per shape on geometric mean, never worse than 1.4x, and better than always
+per shape on geometric mean, never worse than 1.35x, and better than always
 running merge_path; argument errors.  GPU: row statistics equal numpy's,
 and the selected schedule's SpMV is within the FP32 bound.
 """
@@ -44,7 +44,7 @@ def test_model_quality_on_the_sweep(built_lib):
     gm = float(np.exp(np.log(loss).mean()))
     assert len(loss) >= 100
     assert gm <= 1.02, gm
-    assert loss.max() <= 1.4, loss.max()
+    assert loss.max() <= 1.35, loss.max()
     assert gm < float(np.exp(np.log(loss_mp).mean())) - 0.2
 
 
@@ -53,7 +53,7 @@ def test_selection_rules_and_errors(built_lib):
     assert choose(L, 1 << 20, 16_000_000, 100_000)[0] == "merge_path"  # power-law
     assert choose(L, 1 << 22, 1 << 26, 4000)[0] == "merge_path"        # large, skewed
     assert choose(L, 1000, 10_000, 10)[0].startswith("tm")             # small regular
-    assert choose(L, 1 << 22, 1 << 22, 1)[0] == "tm1"                  # one per row
+    assert choose(L, 1 << 20, 1 << 20, 1)[0] == "tm1"                  # one per row
     assert choose(L, 0, 0, 0)[0] in CANDIDATES
     s, t = C.c_int32(), C.c_int32()
     assert L.lib().el_select_schedule(10, 10, 5, 6, C.byref(s), C.byref(t),
