@@ -306,34 +306,10 @@ __device__ __forceinline__ long long warp_merge_search(
   return lo + __popc(__ballot_sync(kFullMask, t));
 }
 
-// The same split with every row end counted as `w` merge items (w >= 1):
-// rows i with offsets[i+1] + w (i + 1) <= diag are closed before diagonal
-// diag.  Returns that count x; the diagonal's nonzero coordinate is
-// min(diag - w x, offsets[x+1]).  w = 1 is warp_merge_search.
-__device__ __forceinline__ long long warp_merge_search_w(
-    const int* __restrict__ row_end, long long rows, long long nnz,
-    long long diag, long long w) {
-  const int lane = threadIdx.x & 31;
-  long long lo = diag > nnz ? (diag - nnz) / w : 0;
-  long long hi = diag / w;
-  if (lo > rows) lo = rows;
-  if (hi > rows) hi = rows;
-  while (hi - lo > 32) {
-    const long long span = hi - lo;
-    const long long p = lo + ((long long)(lane + 1) * span) / 33;
-    const bool t = (long long)__ldg(row_end + p) <= diag - w * (p + 1);
-    const int c = __popc(__ballot_sync(kFullMask, t));
-    const long long plo = __shfl_sync(kFullMask, p, c > 0 ? c - 1 : 0);
-    const long long phi = __shfl_sync(kFullMask, p, c < 32 ? c : 31);
-    if (c > 0) lo = plo + 1;
-    if (c < 32) hi = phi;
-  }
-  const long long p = lo + lane;
-  const bool t = (p < hi) && ((long long)__ldg(row_end + p) <= diag - w * (p + 1));
-  return lo + __popc(__ballot_sync(kFullMask, t));
-}
-
-// Two weighted split points at once (diagonals da and db, rows w items
+// The split with every row end counted as `w` merge items (w >= 1): rows i
+// with offsets[i+1] + w (i + 1) <= diag are closed before diagonal diag, and
+// the diagonal's nonzero coordinate is min(diag - w x, offsets[x+1]) for that
+// count x (w = 1 is warp_merge_search).  Two such split points at once (diagonals da and db, rows w items
 // each), with both searches' probes in flight together.  Also returns
 // offsets[x] and offsets[x+1] of each split row x (row_end = offsets + 1;
 // offsets[rows + 1] reads as nnz), taken from the final probes where they
