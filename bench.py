@@ -607,9 +607,18 @@ def run_batched(args):
     else:
         tdt = torch.bfloat16 if args.value_dtype == "bf16" else torch.float16
         yq = torch.empty_like(y32)
-        items = [(A.quantized(tdt, per_row_scale=not args.no_row_scale), x,
-                  yq[int(rs[m]): int(rs[m]) + A.rows])
-                 for m, (A, x, _) in enumerate(items32)]
+        # quantized values (and scales) of every matrix in one array each, at
+        # the element offsets of its indices (and rows)
+        vq = torch.empty(valc.numel(), dtype=tdt, device=dev)
+        sq = None if args.no_row_scale else torch.empty(y32.numel(), device=dev)
+        rs_l, ns_l = rs.tolist(), ns.tolist()
+        items = []
+        for m, (A, x, _) in enumerate(items32):
+            r0, n0 = int(rs_l[m]), int(ns_l[m])
+            items.append((A.quantized(tdt, per_row_scale=sq is not None,
+                                      out=vq[n0: n0 + A.nnz],
+                                      out_scale=None if sq is None else sq[r0: r0 + A.rows]),
+                          x, yq[r0: r0 + A.rows]))
         plan = api.BatchPlan(items)
         ms = _time_device(plan.execute, args.steps, args.warmup, flush, stream)
         nb = total_bytes(items, 2, not args.no_row_scale)

@@ -95,15 +95,28 @@ class CSR:
         r = int(off.numel() - 1) if rows is None else int(rows)
         return cls(off, idx, val, r, cols)
 
-    def quantized(self, dtype, per_row_scale=True, stream=None):
+    def quantized(self, dtype, per_row_scale=True, stream=None, out=None, out_scale=None):
         """BF16/FP16 copy of an FP32 matrix (el_quantize_values); with
         per_row_scale each row is divided by a power of two that puts its
-        largest magnitude in [1, 2) (BF16) or [2^14, 2^15) (FP16)."""
+        largest magnitude in [1, 2) (BF16) or [2^14, 2^15) (FP16).
+
+        out / out_scale: where to write the values (nnz) and scales (rows),
+        e.g. slices of one array holding many matrices at the same element
+        offsets as their indices -- the kernels load whole tiles with
+        128-bit loads only where indices and values share their position
+        modulo 8 elements."""
         if self.values.dtype != torch.float32:
             raise TypeError("quantize an FP32 matrix")
-        out = torch.empty(self.nnz, dtype=dtype, device=self.device)
-        scale = torch.empty(self.rows, dtype=torch.float32, device=self.device) \
-            if per_row_scale else None
+        if out is None:
+            out = torch.empty(self.nnz, dtype=dtype, device=self.device)
+        if out.dtype != dtype or out.numel() != self.nnz or not out.is_contiguous():
+            raise ValueError("out must be a contiguous tensor of nnz elements of dtype")
+        scale = None
+        if per_row_scale:
+            scale = out_scale if out_scale is not None else \
+                torch.empty(self.rows, dtype=torch.float32, device=self.device)
+            if scale.dtype != torch.float32 or scale.numel() != self.rows:
+                raise ValueError("out_scale must hold rows float32 values")
         L.check(L.lib().el_quantize_values(
             _ptr(self.offsets), self.rows, self.nnz, _ptr(self.values), _DT[dtype],
             _ptr(out), _ptr(scale), _stream(stream)), "el_quantize_values")

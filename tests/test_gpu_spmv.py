@@ -337,3 +337,25 @@ def test_spmv_host_pageable_and_malformed(cuda, oracle_mod):
     with pytest.raises(_lib.ElError) as e:
         api.spmv_host(B, torch.as_tensor(x))
     assert e.value.status == _lib.EL_ERR_MALFORMED_CSR
+
+
+@pytest.mark.parametrize("dtype", [torch.bfloat16, torch.float16])
+def test_quantized_into_slices(cuda, dtype):
+    """quantized(out=, out_scale=) writes the same values and scales as a
+    fresh quantization, into slices of larger arrays."""
+    from edge_loops_gb300 import api
+    rng = np.random.default_rng(71)
+    off, idx, vals, x = random_csr(rng, rows=700, cols=500, max_len=20, empty_frac=0.1)
+    A = dev_csr(off, idx, vals, 500, cuda)
+    ref = A.quantized(dtype, per_row_scale=True)
+    big = torch.zeros(A.nnz + 13, dtype=dtype, device=cuda)
+    bigs = torch.zeros(A.rows + 5, dtype=torch.float32, device=cuda)
+    Q = A.quantized(dtype, per_row_scale=True, out=big[7: 7 + A.nnz],
+                    out_scale=bigs[3: 3 + A.rows])
+    assert torch.equal(Q.values.view(torch.int16), ref.values.view(torch.int16))
+    assert torch.equal(Q.row_scale, ref.row_scale)
+    assert torch.count_nonzero(big[:7].float()) == 0 and torch.count_nonzero(bigs[:3]) == 0
+    y = api.spmv(Q, torch.from_numpy(x).to(cuda)).cpu()
+    assert torch.equal(y, api.spmv(ref, torch.from_numpy(x).to(cuda)).cpu())
+    with pytest.raises(ValueError):
+        A.quantized(dtype, out=big[: A.nnz - 1])
