@@ -127,8 +127,8 @@ def test_edge_cases(cuda, oracle_mod, sched, opts):
 @pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
 def test_merge_path_unaligned_arrays(cuda, oracle_mod, opts, dtype):
     """indices and values starting at every phase modulo 8 elements, equal
-    (vector copies, cells shifted to the common phase) or not (element-wise
-    copies), and arrays that end inside a 16-byte chunk."""
+    (128-bit loads of both) or not (element-wise loads), and arrays that end
+    inside a 16-byte chunk."""
     from edge_loops_gb300 import api
     rng = np.random.default_rng(21)
     off, idx, vals, x = random_csr(rng, rows=3000, cols=5000, max_len=40, empty_frac=0.1,
@@ -138,7 +138,10 @@ def test_merge_path_unaligned_arrays(cuda, oracle_mod, opts, dtype):
     offt = torch.as_tensor(off, device=cuda)
     vq = torch.as_tensor(vals).to(dtype)
     v64 = vq.float().numpy()
-    for si, sv in [(0, 0), (1, 1), (3, 3), (5, 5), (7, 7), (1, 0), (2, 5), (6, 3)]:
+    # equal phases (128-bit loads), and values an odd or an even number of
+    # elements off the indices (element-wise loads)
+    for si, sv in [(0, 0), (1, 1), (3, 3), (5, 5), (7, 7), (1, 0), (2, 5), (6, 3),
+                   (0, 2), (3, 7), (5, 1), (4, 6), (7, 3)]:
         ib = torch.zeros(nnz + 8, dtype=torch.int32, device=cuda)
         vb = torch.zeros(nnz + 8, dtype=dtype, device=cuda)
         ib[si: si + nnz] = torch.as_tensor(idx, device=cuda)
