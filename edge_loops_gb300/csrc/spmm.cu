@@ -101,6 +101,47 @@ __device__ __forceinline__ float column_sum(const Args& a, const VT* vals, const
   return sum;
 }
 
+// sum[j] += A[row, b..e) . B[.., col + j] for NC adjacent columns in one walk
+// of the row: each column's sum still runs in nonzero order (the same
+// roundings as a walk per column), while each index and value is loaded
+// once for the NC columns; W nonzeros per step, the next W indices in flight.
+template <typename VT, typename BT, int W, int NC>
+__device__ __forceinline__ void column_sums(const Args& a, const VT* vals, const BT* B,
+                                            long long b, long long e, int col,
+                                            float (&sum)[NC], bool& bad) {
+#pragma unroll
+  for (int j = 0; j < NC; ++j) sum[j] = 0.f;
+  if (b >= e) return;
+  const unsigned long long cols = (unsigned long long)a.cols;
+  int c[W];
+#pragma unroll
+  for (int k = 0; k < W; ++k) c[k] = b + k < e ? __ldg(a.indices + b + k) : -1;
+  for (long long nz = b;;) {
+    float bv[W][NC], v[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      const bool t = nz + k < e;
+      const bool ok = (unsigned)c[k] < cols;
+      bad |= t && !ok;
+      v[k] = t && ok ? to_f32(vals[nz + k]) : 0.f;
+      const BT* brow = B + (long long)(t && ok ? c[k] : 0) * a.ldb + col;
+#pragma unroll
+      for (int j = 0; j < NC; ++j) bv[k][j] = t && ok ? ld_f32(brow + j) : 0.f;
+    }
+    const long long nn = nz + W;
+#pragma unroll
+    for (int k = 0; k < W; ++k) c[k] = nn + k < e ? __ldg(a.indices + nn + k) : -1;
+#pragma unroll
+    for (int k = 0; k < W; ++k)
+      if (nz + k < e) {
+#pragma unroll
+        for (int j = 0; j < NC; ++j) sum[j] = __fadd_rn(sum[j], __fmul_rn(v[k], bv[k][j]));
+      }
+    if (nn >= e) break;
+    nz = nn;
+  }
+}
+
 // A thread's time is its row's length times the number of columns, so the
 // longest row sets the kernel's: sixteen B loads in flight per step, at
 // three CTAs per SM.
@@ -114,7 +155,14 @@ __global__ void __launch_bounds__(256, 3) thread_mapped_kernel(const Args a) {
     bounds(a, row, &b, &e);
     const float s = a.row_scale ? __ldg(a.row_scale + row) : 1.f;
     bool bad = false;
-    for (int col = 0; col < a.n; ++col) {
+    int col = 0;
+    for (; col + 4 <= a.n; col += 4) {  // four columns per walk of the row
+      float sum[4];
+      column_sums<VT, BT, 8, 4>(a, vals, B, b, e, col, sum, bad);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) a.C[row * a.ldc + col + j] = a.row_scale ? sum[j] * s : sum[j];
+    }
+    for (; col < a.n; ++col) {
       const float sum = column_sum<VT, BT, 16>(a, vals, B, b, e, col, bad);
       a.C[row * a.ldc + col] = a.row_scale ? sum * s : sum;
     }
