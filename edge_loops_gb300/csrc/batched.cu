@@ -160,7 +160,7 @@ __device__ __forceinline__ void rows_nz(const Desc& d, int r0, int r1, int lane,
 }
 
 template <typename VT>
-__global__ void __launch_bounds__(256, 3)
+__global__ void __launch_bounds__(256, mpn::kPer == 16 ? 2 : 3)
     batched_spmv_kernel(const Desc* __restrict__ descs, const Item* __restrict__ items,
                         long long n_items, WsHeader* hdr) {
   __shared__ mpn::WarpSmem<false> smem[8];

@@ -28,10 +28,12 @@
 namespace el {
 namespace mpn {
 
-constexpr int kPer = 8;               // nonzeros per lane
+constexpr int kPer = 8;               // nonzeros per lane: 8 or 16
+constexpr int kPerLog = kPer == 16 ? 4 : 3;
 constexpr int kTileNz = 32 * kPer;    // nonzeros per tile
 constexpr int kMaxEnds = 256;         // row ends per tile (tiles are cut short
                                       // after this many, e.g. empty rows)
+constexpr int kStage = kTileNz > kMaxEnds ? kTileNz : kMaxEnds;  // staging slots per warp
 constexpr int kWarps = 8;
 constexpr int kTPB = 32 * kWarps;
 
@@ -56,26 +58,28 @@ struct Args {
 template <bool COMP>
 struct __align__(16) WarpSmem {
   int re[kMaxEnds];            // end position (tile-local nonzero index) of each row end
-  float yv[kMaxEnds];          // the tile's row sums (or, whole tiles, sums by end position)
-  float yc[COMP ? kMaxEnds : 4];
+  float yv[kStage];            // the tile's row sums (or, whole tiles, sums by end position)
+  float yc[COMP ? kStage : 4];
   unsigned char kp[32][kPer];  // row end closed after lane l's product i (tile-local)
-  unsigned mw[32];             // whole tiles: bit i of word l = a row ends after nonzero 8 l + i
+  unsigned mw[32];             // whole tiles: bit i of word l = a row ends after nonzero kPer l + i
   int pend;
   float pend_s, pend_c;
 };
 
-// 8 consecutive FP32 values (16-byte aligned: two 128-bit loads).
+// kPer consecutive FP32 values (16-byte aligned: 128-bit loads).
 __device__ __forceinline__ void load8(const float* p, float (&v)[kPer]) {
-  const float4 a = __ldcs(reinterpret_cast<const float4*>(p));
-  const float4 b = __ldcs(reinterpret_cast<const float4*>(p) + 1);
-  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-  v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+#pragma unroll
+  for (int k = 0; k < kPer / 4; ++k) {
+    const float4 a = __ldcs(reinterpret_cast<const float4*>(p) + k);
+    v[4 * k] = a.x; v[4 * k + 1] = a.y; v[4 * k + 2] = a.z; v[4 * k + 3] = a.w;
+  }
 }
 __device__ __forceinline__ void load8i(const int* p, int (&c)[kPer]) {
-  const int4 a = __ldcs(reinterpret_cast<const int4*>(p));
-  const int4 b = __ldcs(reinterpret_cast<const int4*>(p) + 1);
-  c[0] = a.x; c[1] = a.y; c[2] = a.z; c[3] = a.w;
-  c[4] = b.x; c[5] = b.y; c[6] = b.z; c[7] = b.w;
+#pragma unroll
+  for (int k = 0; k < kPer / 4; ++k) {
+    const int4 a = __ldcs(reinterpret_cast<const int4*>(p) + k);
+    c[4 * k] = a.x; c[4 * k + 1] = a.y; c[4 * k + 2] = a.z; c[4 * k + 3] = a.w;
+  }
 }
 
 template <typename VT>
@@ -98,8 +102,11 @@ template <typename H>
 struct TileVals16 {
   uint32_t w[kPer / 2];
   __device__ __forceinline__ void load_vec(const H* p) {
-    const uint4 u = __ldcs(reinterpret_cast<const uint4*>(p));
-    w[0] = u.x; w[1] = u.y; w[2] = u.z; w[3] = u.w;
+#pragma unroll
+    for (int k = 0; k < kPer / 8; ++k) {
+      const uint4 u = __ldcs(reinterpret_cast<const uint4*>(p) + k);
+      w[4 * k] = u.x; w[4 * k + 1] = u.y; w[4 * k + 2] = u.z; w[4 * k + 3] = u.w;
+    }
   }
   __device__ __forceinline__ void put(int i, unsigned short h) {
     w[i >> 1] = (i & 1) ? ((w[i >> 1] & 0xffffu) | ((uint32_t)h << 16))
@@ -272,7 +279,7 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
       break;
     }
 
-    // products of this lane's nonzeros 8 lane + i
+    // products of this lane's nonzeros kPer lane + i
     float p[kPer];
     if (fast) {
 #pragma unroll
@@ -303,7 +310,7 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
       // from one ballot, and row r's sum is read back at its end position.
       for (int kk = lane; kk < X; kk += 32) {
         const int P = kk < 32 ? el0 : S.re[kk];
-        if (P > 0) atomicOr(&S.mw[(P - 1) >> 3], 1u << ((P - 1) & 7));
+        if (P > 0) atomicOr(&S.mw[(P - 1) >> kPerLog], 1u << ((P - 1) & (kPer - 1)));
       }
       __syncwarp();
       const unsigned mask = S.mw[lane];
@@ -317,7 +324,7 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
         sc[i] = run.comp();
         if ((mask >> i) & 1u) run = Acc<COMP>();
       }
-      // position q lives at S.yv[(q % 8) * 32 + q / 8]: conflict-free stores
+      // position q lives at S.yv[(q % kPer) * 32 + q / kPer]: conflict-free stores
 #pragma unroll
       for (int i = 0; i < kPer; ++i) {
         S.yv[32 * i + lane] = ss[i];
@@ -359,7 +366,7 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
       for (int kk = lane; kk < X; kk += 32) {  // coalesced store of the tile's rows
         const int P = kk < 32 ? el0 : S.re[kk];
         Acc<COMP> val = carry;
-        const int q = 32 * ((P - 1) & 7) + ((P - 1) >> 3);
+        const int q = 32 * ((P - 1) & (kPer - 1)) + ((P - 1) >> kPerLog);
         if (P > 0) val.set(S.yv[q], COMP ? S.yc[q] : 0.f);
         const int r = ra + kk;
         if (need_lb && r == rs) {
@@ -376,7 +383,7 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
       }
       carry = cout;
     } else {
-      // this lane's row ends: end positions in (8 lane, 8 lane + 8] (lane 0:
+      // this lane's row ends: end positions in (kPer lane, kPer lane + kPer] (lane 0:
       // also position 0, rows closed before any nonzero of the tile)
       int k = 0;
       if (lane > 0) {
@@ -614,7 +621,7 @@ __device__ __forceinline__ void run_range(const Args& a, SmemT& S, const int war
 }
 
 template <typename VT, bool COMP>
-__global__ void __launch_bounds__(kTPB, 3)
+__global__ void __launch_bounds__(kTPB, kPer == 16 ? 2 : 3)
     merge_path_nz_kernel(const Args a) {
   __shared__ WarpSmem<COMP> smem_all[kWarps];
   run_range<VT, COMP, NzWalk>(a, smem_all[threadIdx.x >> 5], kWarps);
