@@ -514,7 +514,7 @@ def _time_device(step, steps, warmup, flush, stream):
 
 
 def run_spmm(args):
-    """SpMM C = A B (BASELINE config 4): A power-law 2^20 x 2^20 with ~8M
+    """SpMM C = A B (the SpMM workload): A power-law 2^20 x 2^20 with ~8M
     nonzeros (Zipf 2.0, cap 100000, seed 3), B dense row-major 2^20 x n."""
     import numpy as np
     import torch
@@ -579,7 +579,7 @@ def run_spmm(args):
 
 
 def run_batched(args):
-    """Batched SpMV (BASELINE config 5): 4096 square CSRs, rows log-uniform in
+    """Batched SpMV (the batched workload): 4096 square CSRs, rows log-uniform in
     [64, 65536], log-normal row lengths (mean 8, sigma 1), seed 4; one
     persistent launch replayed from a CUDA graph.  Also times the plain FP32
     merge-path kernel launched once per matrix (the comparison the target is
