@@ -29,7 +29,7 @@
 // The reference's prepare_gpu() [:228-258] re-points the device atoms at
 // running sums taken in tile order while the device quarks stay in atom
 // order, so with M1 > 1 and K1 < the atom columns its device tiles read
-// other atoms' quarks; this build follows the host-side structure it
+// other atoms' quarks; the partition here follows the host-side structure it
 // builds [:113-124, :162-173], which is what it intends.
 #include <cub/device/device_radix_sort.cuh>
 
