@@ -55,8 +55,20 @@ def _compile(src, verbose):
 
 
 def build(force=False, verbose=False, jobs=None):
-    """Compiles what is out of date and links the library; returns its path."""
+    """Compiles what is out of date and links the library; returns its path.
+    Processes building at the same time (one per rank of a multi-GPU run)
+    take turns on a lock file, so each finds the others' work done."""
     os.makedirs(BUILD, exist_ok=True)
+    import fcntl
+    with open(os.path.join(BUILD, ".lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            return _build_locked(force, verbose, jobs)
+        finally:
+            fcntl.flock(lock, fcntl.LOCK_UN)
+
+
+def _build_locked(force, verbose, jobs):
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     hdr_t = _newest_header()
     todo = []
@@ -73,7 +85,7 @@ def build(force=False, verbose=False, jobs=None):
     objs = [os.path.join(BUILD, os.path.basename(s)[:-3] + ".o") for s in srcs]
     if todo or force or not os.path.exists(LIB) or \
             os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        tmp = LIB + ".tmp"
+        tmp = "%s.tmp%d" % (LIB, os.getpid())
         cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs
         p = subprocess.run(cmd, capture_output=True, text=True)
         if p.returncode != 0:

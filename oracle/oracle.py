@@ -20,7 +20,7 @@ __all__ = [
 def build(force=False):
     """Compiles oracle.c -> liboracle.so with gcc (no FMA contraction)."""
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
-        tmp = LIB + ".tmp"
+        tmp = "%s.tmp%d" % (LIB, os.getpid())
         subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
                                "-pthread", SRC, "-o", tmp, "-lm"])
         os.replace(tmp, LIB)
