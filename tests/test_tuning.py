@@ -1,0 +1,68 @@
+"""Host logic of the two tuning tools (no GPU): tune_select's fit recovers
+the constants of timings made by a known cost model and its choice is the
+cheapest estimate; tune_batch's buckets follow the plan's bucket rules and
+its table text round-trips through JSON."""
+import json
+
+import numpy as np
+import pytest
+
+
+def synthetic_sweep(consts, rng):
+    """Timings of the four candidates on random shapes, exactly as the cost
+    model with `consts` predicts them."""
+    data = []
+    for _ in range(60):
+        rows = int(2 ** rng.uniform(6, 22))
+        per = float(2 ** rng.uniform(0, 8))
+        nnz = int(rows * per)
+        mx = int(min(nnz, per * 2 ** rng.uniform(0, 10)))
+        f = {"rows": rows, "nnz": nnz, "max": mx}
+        a, e = consts["merge_path"]
+        t = {"merge_path": a + e * (nnz + rows) / 1e6}
+        for tpr in (1, 4, 32):
+            a, c, d, e = consts["tm%d" % tpr]
+            t["tm%d" % tpr] = a + c * mx + d * rows / 1e3 + e * nnz / 1e6
+        data.append(("synthetic", f, t))
+    return data
+
+
+def test_select_fit_recovers_a_known_model():
+    pytest.importorskip("scipy")
+    from edge_loops_gb300 import tune_select as ts
+    consts = {"merge_path": (15.0, 4.0), "tm1": (7.0, 0.06, 0.004, 5.6),
+              "tm4": (6.7, 0.044, 0.026, 3.2), "tm32": (6.7, 0.007, 0.2, 1.8)}
+    data = synthetic_sweep(consts, np.random.default_rng(3))
+    model = ts.fit(data)
+    for k, v in consts.items():
+        np.testing.assert_allclose(model[k], v, rtol=1e-6, atol=1e-9)
+    q = ts.quality(data, lambda f: ts.predict(model, f))
+    assert q["geomean"] == pytest.approx(1.0) and q["worst"] == pytest.approx(1.0)
+    assert q["shapes"] == len(data)
+    # always merge_path is worse on this data, and quality says so
+    assert ts.quality(data, lambda f: "merge_path")["geomean"] > 1.0
+
+
+def test_select_predict_takes_the_cheapest_estimate():
+    from edge_loops_gb300 import tune_select as ts
+    model = {"merge_path": (15.0, 4.0), "tm1": (7.0, 0.1, 0.0, 6.0),
+             "tm4": (7.0, 0.05, 0.02, 3.0), "tm32": (7.0, 0.01, 0.2, 2.0)}
+    assert ts.predict(model, {"rows": 1000, "nnz": 10000, "max": 10}).startswith("tm")
+    assert ts.predict(model, {"rows": 1 << 20, "nnz": 16_000_000, "max": 100_000}) == \
+        "merge_path"
+
+
+def test_batch_buckets_and_table_text():
+    from edge_loops_gb300 import _lib as L
+    from edge_loops_gb300 import tune_batch as tb
+    # rows: bucket b holds [2^b, 2^(b+1)), the last one everything above
+    assert [tb.row_bucket(r) for r in (1, 2, 3, 4, 7, 8)] == [0, 1, 1, 2, 2, 3]
+    assert tb.row_bucket(1 << 40) == L.EL_BATCH_ROW_BUCKETS - 1
+    # mean row length: 0 below 1, then one bucket per power of two
+    assert [tb.len_bucket(a) for a in (0.5, 1.0, 1.9, 2.0, 3.9, 4.0)] == [0, 1, 1, 2, 2, 3]
+    assert tb.len_bucket(1e9) == L.EL_BATCH_LEN_BUCKETS - 1
+    assert [tb.cv_bucket(c) for c in (0.0, 0.25, 0.74, 0.75, 1.49, 1.5, 9.0)] == \
+        [0, 1, 1, 2, 2, 3, 3]
+    table = {"threads_per_row": [1, 2], "entries": {"3,4,1": [64, 12], "0,1,0": [4, 10]},
+             "note": "x"}
+    assert json.loads(tb.dumps(table)) == table
