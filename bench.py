@@ -225,7 +225,7 @@ def run_ours(args, rank, world):
     check = verify(args, A, x, y, W)
 
     # ---- e2e through the C ABI with host buffers
-    e2e = run_e2e(args, A, W, nbytes, dev)
+    e2e = run_e2e(args, A, W, nbytes, dev, world)
 
     peak, peak_kind = measured_peaks()
     achieved = nbytes / (ms_per_step * 1e-3) / 1e9
@@ -306,12 +306,14 @@ def verify(args, A, x, y, W):
     return out
 
 
-def run_e2e(args, A, W, nbytes, dev):
+def run_e2e(args, A, W, nbytes, dev, world=1):
     """The same metric through the C ABI with host buffers (pinned): per step
     the matrix, x and y cross the host link inside the timed region.
     `value`: el_spmv_host (row blocks copied on a second stream while the
     previous block is multiplied, y blocks copied back); also reported: the
-    plain sequence of H2D copies, el_spmv and the D2H copy of y."""
+    plain sequence of H2D copies, el_spmv and the D2H copy of y.  With
+    several ranks every timing starts after a barrier, the slowest rank's
+    time counts, and value and bytes are the whole job's."""
     import numpy as np
     import torch
     import oracle
@@ -356,6 +358,9 @@ def run_e2e(args, A, W, nbytes, dev):
         steps = max(5, min(args.steps, 50))
         s = torch.cuda.Event(enable_timing=True)
         e = torch.cuda.Event(enable_timing=True)
+        if world > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
         s.record(stream)
         for _ in range(steps):
             step()
@@ -363,7 +368,11 @@ def run_e2e(args, A, W, nbytes, dev):
         torch.cuda.synchronize()
         if ws.errors():
             raise SystemExit("device error flags in the e2e run")
-        return s.elapsed_time(e) / steps, steps
+        ms = s.elapsed_time(e)
+        if world > 1:
+            from edge_loops_gb300.dist import max_over_ranks
+            ms = max_over_ranks(ms, device=dev)
+        return ms / steps, steps
 
     ms_copy, _ = timed(step_copy)
     ms, steps = timed(step_stream)
@@ -378,11 +387,11 @@ def run_e2e(args, A, W, nbytes, dev):
     bad = int(np.sum(np.abs(h_y.numpy().astype(np.float64) - y64) > (n * u / (1 - n * u)) * yabs))
     if bad:
         raise SystemExit(f"el_spmv_host output fails the oracle bound in {bad} rows")
-    return {"value": round(nbytes / (ms * 1e-3) / 1e9, 2), "unit": "GB/s",
+    return {"value": round(world * nbytes / (ms * 1e-3) / 1e9, 2), "unit": "GB/s",
             "ms_per_step": round(ms, 4), "steps": steps,
-            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "h2d_bytes_per_step": int(world * h2d), "d2h_bytes_per_step": int(world * d2h),
             "api": "el_spmv_host (row blocks streamed, copies overlapped with the SpMV)",
-            "copy_then_spmv": {"value": round(nbytes / (ms_copy * 1e-3) / 1e9, 2),
+            "copy_then_spmv": {"value": round(world * nbytes / (ms_copy * 1e-3) / 1e9, 2),
                                "ms_per_step": round(ms_copy, 4)},
             "rows_outside_fp32_bound": bad}
 
