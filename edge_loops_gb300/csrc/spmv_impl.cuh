@@ -118,10 +118,32 @@ struct SpmvImpl {
   }
 
   static constexpr int kWoTpb = 128;
+  static constexpr long long kWoShare = 256;    // merge items per thread aimed at
+  static constexpr long long kWoMinShare = 32;  // merge items per thread, at least
+  static constexpr int kWoBlocksPerSm = 16;     // at most this many blocks per SM
   static long long wo_num_threads(const SpmvCall& c) {
     if (c.o.num_threads > 0) return c.o.num_threads;
-    // the reference launches 2 x SM count blocks of 128
-    return 2LL * device_info(c.device).sm_count * kWoTpb;
+    // The reference launches 2 x SM count blocks of 128, so each thread walks
+    // thousands of items one latency chain at a time.  Here: every resident
+    // block, and more (one thread per kWoShare items, up to kWoBlocksPerSm
+    // blocks per SM) on large merges -- blocks take their ids from a ticket,
+    // so a look-back only waits on blocks already running -- but no thread
+    // with fewer than kWoMinShare items, since each share pays two global
+    // merge-path searches.
+    const long long blk_items = kWoShare * kWoTpb, min_items = kWoMinShare * kWoTpb;
+    const long long total = c.A.rows + c.A.nnz;
+    const long long sms = device_info(c.device).sm_count;
+    const void* k = c.o.compensated ? (const void*)work_oriented_spmv_kernel<VT, kWoTpb, true>
+                                    : (const void*)work_oriented_spmv_kernel<VT, kWoTpb, false>;
+    const int per_sm = resident_ctas_per_sm(k, kWoTpb, 0);
+    long long nb = (long long)(per_sm > 2 ? per_sm : 2) * sms;
+    const long long share = (total + blk_items - 1) / blk_items;
+    if (share > nb) nb = share;
+    if (nb > kWoBlocksPerSm * sms) nb = kWoBlocksPerSm * sms;
+    const long long most = (total + min_items - 1) / min_items;
+    if (nb > most) nb = most;
+    if (nb < 1) nb = 1;
+    return nb * kWoTpb;
   }
   static long long work_oriented_slots(const SpmvCall& c) {
     return (wo_num_threads(c) + kWoTpb - 1) / kWoTpb;

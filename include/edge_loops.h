@@ -145,9 +145,12 @@ typedef struct el_spmv_opts {
   int32_t group_rows;        /* group_mapped: rows per group: 32 (one warp
                                 per group, the reference's warp_mapped) or
                                 threads_per_block (block_mapped) */
-  int64_t num_threads;       /* work_oriented: threads of the even split
-                                (the reference uses 2 x SMs x 128); 0 =
-                                resident capacity */
+  int64_t num_threads;       /* work_oriented: threads of the even split,
+                                a multiple of 128 (the reference uses
+                                2 x SMs x 128); 0 = the resident blocks'
+                                threads, or one per 256 merge items when
+                                that is more (at most 16 x SMs x 128), and
+                                none with fewer than 32 merge items */
   int32_t compensated;       /* 1: Neumaier / two-sum compensated FP32 sums */
   int32_t max_ctas;          /* cap on persistent grids (0 = resident) */
   int32_t wait_limit_us;     /* bound on every device-side wait (0 = 2 s) */

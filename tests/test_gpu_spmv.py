@@ -24,6 +24,7 @@ SCHEDS = [
     ("merge_path_flat", {"variant": 1, "items_per_thread": 4}),
     ("merge_path_flat", {"variant": 1, "compensated": True}),
     ("work_oriented", {}),
+    ("work_oriented", {"num_threads": 1024}),
     ("thread_mapped", {}),
     ("thread_mapped", {"threads_per_row": 8}),
     ("thread_mapped", {"threads_per_row": 32}),
