@@ -39,6 +39,24 @@ def _stream(stream):
     return C.c_void_p(s.cuda_stream)
 
 
+def _check_vector(name, t, device, n, dtype=torch.float32):
+    """t must be a contiguous `dtype` tensor of at least n entries on `device`
+    (the library reads n entries from its first element)."""
+    if t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype}")
+    if t.device != device:
+        raise ValueError(f"{name} is on {t.device}, the matrix on {device}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    if t.numel() < n:
+        raise ValueError(f"{name} holds {t.numel()} entries, needs {n}")
+
+
+def _check_on_gpu(A):
+    if A.device.type != "cuda":
+        raise ValueError("the matrix is in host memory: use spmv_host, or move it to the GPU")
+
+
 def _sched(schedule):
     if isinstance(schedule, int):
         return schedule
@@ -61,8 +79,24 @@ class CSR:
         self.rows = int(rows)
         self.cols = int(cols)
         self.row_scale = row_scale
+        # the library reads these as plain arrays from their first element
         if values.dtype not in _DT:
             raise TypeError(f"values dtype {values.dtype} not supported")
+        if offsets.dtype != torch.int32 or indices.dtype != torch.int32:
+            raise TypeError("offsets and indices must be int32")
+        if row_scale is not None and row_scale.dtype != torch.float32:
+            raise TypeError("row_scale must be float32")
+        arrays = [offsets, indices, values] + ([row_scale] if row_scale is not None else [])
+        if any(t.device != offsets.device for t in arrays):
+            raise ValueError("offsets, indices, values and row_scale must be on one device")
+        if not all(t.is_contiguous() for t in arrays):
+            raise ValueError("offsets, indices, values and row_scale must be contiguous")
+        if self.rows < 0 or self.cols < 0 or offsets.numel() < self.rows + 1:
+            raise ValueError("offsets must hold rows + 1 entries")
+        if values.numel() < indices.numel():
+            raise ValueError("values must hold an entry per index")
+        if row_scale is not None and row_scale.numel() < self.rows:
+            raise ValueError("row_scale must hold an entry per row")
 
     @property
     def nnz(self):
@@ -181,12 +215,11 @@ def make_opts(threads_per_block=0, items_per_thread=0, threads_per_row=0, group_
 def spmv(A, x, y=None, schedule="merge_path_flat", stream=None, workspace=None, **opts):
     """y = A x (y overwritten), the reference's
     loops::algorithms::spmv::<schedule>(csr, x, y, stream)."""
+    _check_on_gpu(A)
+    _check_vector("x", x, A.device, A.cols)
     if y is None:
         y = torch.empty(A.rows, dtype=torch.float32, device=A.device)
-    if x.dtype != torch.float32 or y.dtype != torch.float32:
-        raise TypeError("x and y are float32")
-    if x.numel() < A.cols or y.numel() < A.rows:
-        raise ValueError("x or y too short")
+    _check_vector("y", y, A.device, A.rows)
     a = A.el()
     o = make_opts(**opts)
     L.check(L.lib().el_spmv(_ws(workspace), C.byref(a), _sched(schedule), C.byref(o),
@@ -224,14 +257,12 @@ def spmv_host(A, x, y=None, schedule="merge_path_flat", block_nnz=0, stream=None
     memory, streamed to the current GPU in row blocks that overlap the copies
     with the SpMV.  Pin the tensors (`.pin_memory()`) for full link speed.
     Asynchronous: synchronise the stream before reading y or reusing A, x."""
-    if A.offsets.is_cuda or x.is_cuda:
-        raise ValueError("spmv_host takes host (CPU) tensors")
+    if A.offsets.is_cuda:
+        raise ValueError("spmv_host takes a matrix in host (CPU) memory")
+    _check_vector("x", x, A.device, A.cols)
     if y is None:
         y = torch.empty(A.rows, dtype=torch.float32).pin_memory()
-    if x.dtype != torch.float32 or y.dtype != torch.float32 or y.is_cuda:
-        raise TypeError("x and y are float32 host tensors")
-    if x.numel() < A.cols or y.numel() < A.rows:
-        raise ValueError("x or y too short")
+    _check_vector("y", y, A.device, A.rows)
     a = A.el()
     o = make_opts(**opts)
     L.check(L.lib().el_spmv_host(_ws(workspace), C.byref(a), _sched(schedule), C.byref(o),
@@ -291,13 +322,17 @@ def csr_from_coo(rows, cols, row_indices, col_indices, values, device=None, stre
 def spmm(A, B, Cm=None, schedule="merge_path_flat", stream=None, workspace=None, **opts):
     """C = A B with B row-major (cols x n) float32/bfloat16/float16 and C
     float32 (rows x n), the reference's loops::algorithms::spmm."""
-    if B.dim() != 2 or B.shape[0] != A.cols or B.stride(1) != 1:
+    _check_on_gpu(A)
+    if B.dim() != 2 or B.shape[0] != A.cols or B.stride(1) != 1 or B.stride(0) < B.shape[1]:
         raise ValueError("B must be a row-major (cols x n) matrix")
+    if B.dtype not in _DT or B.device != A.device:
+        raise ValueError("B must be float32/bfloat16/float16 on the matrix's device")
     n = B.shape[1]
     if Cm is None:
         Cm = torch.empty(A.rows, n, dtype=torch.float32, device=A.device)
-    if Cm.dtype != torch.float32 or Cm.stride(1) != 1 or Cm.shape != (A.rows, n):
-        raise ValueError("C must be float32 row-major (rows x n)")
+    if Cm.dtype != torch.float32 or Cm.stride(1) != 1 or Cm.shape != (A.rows, n) or \
+            Cm.stride(0) < n or Cm.device != A.device:
+        raise ValueError("C must be float32 row-major (rows x n) on the matrix's device")
     a = A.el()
     o = make_opts(**opts)
     L.check(L.lib().el_spmm(_ws(workspace), C.byref(a), _sched(schedule), C.byref(o),

@@ -168,3 +168,48 @@ def test_batched_generator():
     assert total == idxc.numel()
     mean = idxc.numel() / float(R.sum())
     assert 6.0 < mean < 10.0
+
+
+def test_python_api_rejects_arrays_the_library_cannot_read():
+    """The library reads every array as plain memory from its first element,
+    so the Python face refuses what would read the wrong bytes or past an
+    allocation: wrong dtypes, strided or expanded views, short arrays, mixed
+    devices, and a host matrix handed to the device entry points."""
+    import torch
+    from edge_loops_gb300 import api
+    off = torch.tensor([0, 2, 3], dtype=torch.int32)
+    idx = torch.tensor([0, 2, 1], dtype=torch.int32)
+    val = torch.tensor([1.0, 2.0, 3.0])
+    A = api.CSR(off, idx, val, 2, 3)
+    assert A.nnz == 3 and A.device.type == "cpu"
+    with pytest.raises(TypeError):
+        api.CSR(off.long(), idx, val, 2, 3)
+    with pytest.raises(TypeError):
+        api.CSR(off, idx.long(), val, 2, 3)
+    with pytest.raises(TypeError):
+        api.CSR(off, idx, val.double(), 2, 3)
+    with pytest.raises(TypeError):
+        api.CSR(off, idx, val, 2, 3, row_scale=torch.ones(2, dtype=torch.float64))
+    with pytest.raises(ValueError):  # strided view
+        api.CSR(off, torch.tensor([0, 9, 2, 9, 1, 9], dtype=torch.int32)[::2], val, 2, 3)
+    with pytest.raises(ValueError):  # expanded (stride 0): one element of storage
+        api.CSR(off, idx, torch.ones(1).expand(3), 2, 3)
+    with pytest.raises(ValueError):
+        api.CSR(off, idx, val, 3, 3)  # offsets too short for 3 rows
+    with pytest.raises(ValueError):
+        api.CSR(off, idx, val[:2], 2, 3)  # fewer values than indices
+    with pytest.raises(ValueError):
+        api.CSR(off, idx, val, 2, 3, row_scale=torch.ones(1))
+    x = torch.ones(3)
+    with pytest.raises(ValueError):  # device entry point, host matrix
+        api.spmv(A, x)
+    with pytest.raises(ValueError):
+        api.spmm(A, torch.ones(3, 4))
+    with pytest.raises(ValueError):  # x shorter than cols
+        api.spmv_host(A, torch.ones(2))
+    with pytest.raises(ValueError):  # expanded x
+        api.spmv_host(A, torch.ones(1).expand(3))
+    with pytest.raises(TypeError):
+        api.spmv_host(A, torch.ones(3, dtype=torch.float64))
+    with pytest.raises(ValueError):  # y strided
+        api.spmv_host(A, x, torch.empty(4)[::2])
