@@ -107,9 +107,15 @@ class ClockSampler:
             self.proc.kill()
         if self.thread:
             self.thread.join(timeout=2)
+        return self.summarize(self.lines)
+
+    @staticmethod
+    def summarize(lines):
+        """Median SM clock, highest max clock and the throttle reasons seen
+        Active, from nvidia-smi CSV lines in FIELDS order (others skipped)."""
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in lines:
             f = [t.strip() for t in ln.split(",")]
             if len(f) < 9:
                 continue
