@@ -912,17 +912,17 @@ def main():
     if world > 1:
         torch.distributed.init_process_group(
             "nccl", device_id=torch.device("cuda", _env_int("LOCAL_RANK", 0)))
-    if args.workload in ("spmm_powerlaw", "spmv_batched", "csr_build", "spmv_edge"):
-        line = {"spmm_powerlaw": run_spmm, "spmv_batched": run_batched,
-                "csr_build": run_csr_build, "spmv_edge": run_edge}[args.workload](args)
+    try:
+        if args.workload in ("spmm_powerlaw", "spmv_batched", "csr_build", "spmv_edge"):
+            line = {"spmm_powerlaw": run_spmm, "spmv_batched": run_batched,
+                    "csr_build": run_csr_build, "spmv_edge": run_edge}[args.workload](args)
+        else:
+            line = run_ours(args, rank, world)
         if rank == 0:
             print(json.dumps(line))
-        return
-    line = run_ours(args, rank, world)
-    if rank == 0:
-        print(json.dumps(line))
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    finally:
+        if world > 1:
+            torch.distributed.destroy_process_group()
 
 
 if __name__ == "__main__":
