@@ -316,8 +316,8 @@ el_status el_batch_plan_create(const el_batch_item* items, int32_t count,
     const el_csr& A = items[i].A;
     if (A.rows < 0 || A.cols < 0 || A.nnz < 0)
       return fail(EL_ERR_INVALID_ARGUMENT, "matrix %d: negative size", i);
-    if (A.rows + A.nnz >= (1LL << 31) || A.cols >= (1LL << 31))
-      return fail(EL_ERR_OVERFLOW, "matrix %d: rows+nnz >= 2^31", i);
+    if (A.rows + A.nnz >= kMergeLimit || A.cols >= (1LL << 31))
+      return fail(EL_ERR_OVERFLOW, "matrix %d: rows+nnz >= 2^31 - 2^16", i);
     if (A.value_dtype != dtype)
       return fail(EL_ERR_UNSUPPORTED, "matrix %d: all matrices of a plan share one dtype", i);
     if (A.value_dtype < EL_F32 || A.value_dtype > EL_F16)

@@ -173,10 +173,10 @@ el_status check_csr(const el_csr* A) {
   if (A->rows < 0 || A->cols < 0 || A->nnz < 0)
     return fail(EL_ERR_INVALID_ARGUMENT, "negative size (rows=%lld cols=%lld nnz=%lld)",
                 (long long)A->rows, (long long)A->cols, (long long)A->nnz);
-  if (A->rows + A->nnz >= (1LL << 31) || A->cols >= (1LL << 31))
+  if (A->rows + A->nnz >= kMergeLimit || A->cols >= (1LL << 31))
     return fail(EL_ERR_OVERFLOW,
-                "rows+nnz = %lld needs 64-bit merge coordinates (limit 2^31-1, as "
-                "the reference's int32 search)",
+                "rows+nnz = %lld needs 64-bit merge coordinates (limit 2^31 - 2^16: the "
+                "reference's int32 search, less headroom for tile arithmetic)",
                 (long long)(A->rows + A->nnz));
   if (A->value_dtype < EL_F32 || A->value_dtype > EL_F16)
     return fail(EL_ERR_INVALID_ARGUMENT, "unknown value dtype %d", A->value_dtype);
@@ -484,7 +484,7 @@ el_status el_merge_path_partition(const int32_t* offsets, int64_t rows, int64_t 
                                   el_stream_t stream) {
   if (rows < 0 || nnz < 0 || tpb <= 0 || ipt <= 0)
     return fail(EL_ERR_INVALID_ARGUMENT, "bad partition arguments");
-  if (rows + nnz >= (1LL << 31)) return fail(EL_ERR_OVERFLOW, "rows+nnz >= 2^31");
+  if (rows + nnz >= kMergeLimit) return fail(EL_ERR_OVERFLOW, "rows+nnz >= 2^31 - 2^16");
   if (rows == 0) return fail(EL_ERR_INVALID_ARGUMENT, "rows == 0");
   if (!offsets || !coords) return fail(EL_ERR_NULL_POINTER, "offsets/coords is NULL");
   return launch_partition_tiles(offsets, rows, nnz, (int64_t)tpb * ipt, coords,
@@ -496,7 +496,7 @@ el_status el_merge_path_thread_coords(const int32_t* offsets, int64_t rows, int6
                                       el_stream_t stream) {
   if (rows <= 0 || nnz < 0 || tpb < 2 || tpb > 1024 || ipt <= 0 || ipt > 64)
     return fail(EL_ERR_INVALID_ARGUMENT, "bad partition arguments");
-  if (rows + nnz >= (1LL << 31)) return fail(EL_ERR_OVERFLOW, "rows+nnz >= 2^31");
+  if (rows + nnz >= kMergeLimit) return fail(EL_ERR_OVERFLOW, "rows+nnz >= 2^31 - 2^16");
   if (!offsets || !coords) return fail(EL_ERR_NULL_POINTER, "offsets/coords is NULL");
   return launch_partition_threads(offsets, rows, nnz, tpb, ipt, coords,
                                   (cudaStream_t)stream);
@@ -507,7 +507,7 @@ el_status el_work_oriented_partition(const int32_t* offsets, int64_t rows, int64
                                      el_stream_t stream) {
   if (rows <= 0 || nnz < 0 || num_threads <= 0)
     return fail(EL_ERR_INVALID_ARGUMENT, "bad partition arguments");
-  if (rows + nnz >= (1LL << 31)) return fail(EL_ERR_OVERFLOW, "rows+nnz >= 2^31");
+  if (rows + nnz >= kMergeLimit) return fail(EL_ERR_OVERFLOW, "rows+nnz >= 2^31 - 2^16");
   if (!offsets || !coords) return fail(EL_ERR_NULL_POINTER, "offsets/coords is NULL");
   return launch_partition_work_oriented(offsets, rows, nnz, num_threads, coords,
                                         (cudaStream_t)stream);

@@ -10,6 +10,11 @@
 
 namespace el {
 
+// Largest rows + nnz (merge-path length) accepted: int32 merge coordinates as
+// in the reference's search, less 2^16 of headroom so that a coordinate plus
+// a tile's extent (at most a few thousand items) never leaves int32.
+constexpr long long kMergeLimit = (1LL << 31) - (1LL << 16);
+
 // Records a failure for el_last_error_string() and returns `s`.
 el_status fail(el_status s, const char* fmt, ...);
 // EL_OK on cudaSuccess, else EL_ERR_CUDA with the CUDA error text.

@@ -630,12 +630,12 @@ __global__ void __launch_bounds__(kTPB, kPer == 16 ? 2 : 3)
 // Merge items per row end for the warp ranges: a row end costs the walk
 // about as much as two nonzeros (its ballot, bit, staging and store), so
 // ranges of short rows get fewer items.  Falls back to 1 where the weighted
-// merge length would not fit 31 bits.
+// merge length would reach kMergeLimit.
 constexpr int kDefaultRowWeight = 2;
 inline int row_weight(const SpmvCall& c) {
   int w = c.o.row_weight > 0 ? c.o.row_weight : kDefaultRowWeight;
   if (w > 16) w = 16;
-  if ((long long)w * c.A.rows + c.A.nnz >= (1LL << 31)) w = 1;
+  if ((long long)w * c.A.rows + c.A.nnz >= kMergeLimit) w = 1;
   return w;
 }
 

@@ -86,8 +86,8 @@ extern "C" el_status el_spmv_static_scratch(const el_csr* A, const float* x, flo
   if (!A) return fail(EL_ERR_NULL_POINTER, "A is NULL");
   if (A->rows < 0 || A->cols < 0 || A->nnz < 0)
     return fail(EL_ERR_INVALID_ARGUMENT, "negative size");
-  if (A->rows + A->nnz >= (1LL << 31) || A->cols >= (1LL << 31))
-    return fail(EL_ERR_OVERFLOW, "rows+nnz = %lld: the merge path is int32 (limit 2^31-1)",
+  if (A->rows + A->nnz >= kMergeLimit || A->cols >= (1LL << 31))
+    return fail(EL_ERR_OVERFLOW, "rows+nnz = %lld: the merge path is int32 (limit 2^31 - 2^16)",
                 (long long)(A->rows + A->nnz));
   if (A->value_dtype < EL_F32 || A->value_dtype > EL_F16)
     return fail(EL_ERR_INVALID_ARGUMENT, "unknown value dtype %d", A->value_dtype);

@@ -83,7 +83,8 @@ typedef enum el_status {
   EL_OK = 0,
   EL_ERR_INVALID_ARGUMENT = 1, /* bad size, dtype, schedule option */
   EL_ERR_NULL_POINTER = 2,     /* a required pointer is NULL */
-  EL_ERR_OVERFLOW = 3,         /* rows+nnz >= 2^31 (int32 merge path) */
+  EL_ERR_OVERFLOW = 3,         /* rows+nnz >= 2^31 - 2^16 (int32 merge
+                                  path with headroom for tile arithmetic) */
   EL_ERR_UNSUPPORTED = 4,      /* e.g. the reference's unimplemented
                                   `bucketing` schedule */
   EL_ERR_MALFORMED_CSR = 5,    /* el_csr_validate found a defect */

@@ -84,6 +84,9 @@ def test_argument_errors_without_gpu(built_lib):
     a = _csr(1 << 30, 10, 1 << 30)
     assert L.el_spmv(None, C.byref(a), 0, None, x, y, None) == _lib.EL_ERR_OVERFLOW
     assert b"2^31" in L.el_last_error_string()
+    # the limit keeps 2^16 of headroom below 2^31 for tile arithmetic
+    a = _csr(3, 10, (1 << 31) - (1 << 16) - 3)
+    assert L.el_spmv(None, C.byref(a), 0, None, x, y, None) == _lib.EL_ERR_OVERFLOW
     a = _csr(10, 10, -1)
     assert L.el_spmv(None, C.byref(a), 0, None, x, y, None) == _lib.EL_ERR_INVALID_ARGUMENT
     a = _csr(10, 10, 5, dtype=7)
