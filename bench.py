@@ -378,8 +378,9 @@ def run_e2e(args, A, W, nbytes, dev, world=1):
         h2d += h_sc.numel() * 4
     d2h = h_y.numel() * 4
 
-    def step_stream(block_nnz=0):
-        api.spmv_host(Ah, h_x, h_y, schedule=args.schedule, workspace=ws, block_nnz=block_nnz)
+    def step_stream():
+        api.spmv_host(Ah, h_x, h_y, schedule=args.schedule, workspace=ws,
+                      block_nnz=args.e2e_block_nnz)
 
     def step_copy():
         d_off.copy_(h_off, non_blocking=True)
@@ -431,6 +432,7 @@ def run_e2e(args, A, W, nbytes, dev, world=1):
             "ms_per_step": round(ms, 4), "steps": steps,
             "h2d_bytes_per_step": int(world * h2d), "d2h_bytes_per_step": int(world * d2h),
             "api": "el_spmv_host (row blocks streamed, copies overlapped with the SpMV)",
+            "block_nnz": args.e2e_block_nnz,
             "copy_then_spmv": {"value": round(world * nbytes / (ms_copy * 1e-3) / 1e9, 2),
                                "ms_per_step": round(ms_copy, 4)},
             "rows_outside_fp32_bound": bad}
@@ -890,6 +892,8 @@ def main():
     ap.add_argument("--n", type=int, default=128, help="SpMM: columns of B")
     ap.add_argument("--b-dtype", default="f32", choices=["f32", "bf16", "f16"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--e2e-block-nnz", type=int, default=0,
+                    help="e2e: nonzeros per streamed row block (0: the library's default)")
     ap.add_argument("--edge", default="pos:256:1",
                     help="spmv_edge partition: pos:P:T or coord:M0:K0:M1:K1")
     args = ap.parse_args()
