@@ -379,7 +379,8 @@ class setup<algorithms_t::group_mapped, THREADS_PER_BLOCK, THREADS_PER_TILE, til
     return tiles_t(lo - 1);
   }
   __device__ __forceinline__ bool is_valid_accessor(tiles_t& v_tile, partition_t& p) {
-    return v_tile >= tiles_t(0) && (long long)v_tile < (long long)length(p);
+    const long long t = (long long)v_tile;
+    return t >= 0 && t < (long long)length(p);
   }
   // the global row of group-local row v_tile
   __device__ __forceinline__ tiles_t tile_id(tiles_t& v_tile, partition_t& p) {
