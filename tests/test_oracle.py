@@ -148,3 +148,35 @@ def test_spmm_loop(oracle_mod):
     for c in range(7):
         y64, ya = oracle_mod.spmv_f64(off, idx, vals, B[:, c])
         np.testing.assert_allclose(C64[:, c], y64, rtol=1e-15, atol=1e-300)
+
+
+def test_split_points_property_random_shapes(oracle_mod):
+    """Property check over many random row-length patterns (empty rows, one
+    row, no nonzeros, long rows): the restated search, the tile split and the
+    work_oriented split all land on the brute-force merge walk."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+
+    @hyp.settings(max_examples=150, deadline=None, derandomize=True)
+    @hyp.given(lens=st.lists(st.integers(0, 12), min_size=1, max_size=40),
+               items=st.integers(1, 9), nt=st.integers(1, 23))
+    def check(lens, items, nt):
+        off = np.zeros(len(lens) + 1, dtype=np.int32)
+        off[1:] = np.cumsum(lens)
+        rows, nnz = len(lens), int(off[-1])
+        total = rows + nnz
+        walk = oracle_mod.merge_path_walk(off, nnz, 1)
+        assert len(walk) == total + 1
+        for d in range(total + 1):
+            assert oracle_mod.mp_search(d, off[1:], rows, 0, nnz) == tuple(walk[d])
+        tiles = oracle_mod.merge_path_tile_coords(off, nnz, items)
+        for t in range(len(tiles)):
+            assert tuple(tiles[t]) == tuple(walk[min(t * items, total)])
+        c = oracle_mod.work_oriented_coords(off, nnz, nt)
+        wpt = -(-total // nt)
+        for t in range(nt):
+            up = min(wpt * t, total)
+            assert tuple(c[t, :2]) == tuple(walk[up])
+            assert tuple(c[t, 2:]) == tuple(walk[min(up + wpt, total)])
+
+    check()
