@@ -16,7 +16,9 @@ every step.  The metric is achieved bandwidth in GB/s of the algorithmic
 `value` is timed on the device with CUDA events around every SpMV launch
 (inputs resident in HBM); `e2e` is the same metric through the C ABI call
 with host buffers, the H2D copy of the matrix and x (pinned memory) and the
-D2H copy of y inside the timed region.  `--impl reference` times the
+D2H copy of y inside the timed region (row blocks of --e2e-block-nnz
+nonzeros, default the library's); `graph_replay` times 100 SpMVs captured
+in one CUDA graph and replayed without L2 flushes between them.  `--impl reference` times the
 reference's CPU SpMV loop (examples/spmv/helpers.hxx:106-112, restated in
 oracle/oracle.c, rows split over every host core) on the same workload.
 
