@@ -6,7 +6,9 @@
 // (docs/loadbalancing_api.md; include/loops/schedule.hxx:21-46,
 // stride_ranges.hxx:16-64, schedule/thread_mapped.hxx:88-166,
 // schedule/work_oriented.hxx:86-195, schedule/group_mapped.hxx:80-250)
-// compiles against this header unchanged:
+// compiles against this header unchanged (it also replaces
+// <loops/util/math.hxx> and <loops/util/launch.hxx>: math::ceil_div,
+// launch::non_cooperative, launch::cooperative):
 //
 //   for (auto i : loops::grid_stride_range(0, n)) ...            // ranges
 //
@@ -138,6 +140,36 @@ template <typename T>
 __device__ __forceinline__ step_range_t<T> custom_stride_range(T begin, T end, T stride) {
   return stepped_range<T>(begin, end, stride);
 }
+
+// ---- helpers the reference's kernels and launchers use
+// (util/math.hxx:26-31, util/launch.hxx:40-74)
+namespace math {
+// n / d rounded up
+template <class numerator_t, class denominator_t>
+__host__ __device__ __forceinline__ constexpr numerator_t ceil_div(numerator_t const& n,
+                                                                   denominator_t const& d) {
+  return static_cast<numerator_t>(n / d + (n % d != 0 ? 1 : 0));
+}
+}  // namespace math
+
+namespace launch {
+// kernel<<<blocks, threads, 0, stream>>>(args...)
+template <typename func_t, typename... args_t>
+void non_cooperative(cudaStream_t stream, const func_t& kernel, dim3 number_of_blocks,
+                     dim3 threads_per_block, args_t&&... args) {
+  kernel<<<number_of_blocks, threads_per_block, 0, stream>>>(static_cast<args_t&&>(args)...);
+}
+// the same as a cooperative launch (every block resident at once; the
+// caller sizes the grid to fit)
+template <typename func_t, typename... args_t>
+cudaError_t cooperative(cudaStream_t stream, const func_t& kernel, std::size_t number_of_blocks,
+                        std::size_t threads_per_block, args_t&&... args) {
+  void* arg_addresses[sizeof...(args_t) > 0 ? sizeof...(args_t) : 1] = {
+      const_cast<void*>(static_cast<const void*>(&args))...};
+  return cudaLaunchCooperativeKernel((const void*)kernel, dim3((unsigned)number_of_blocks),
+                                     dim3((unsigned)threads_per_block), arg_addresses, 0, stream);
+}
+}  // namespace launch
 
 namespace schedule {
 

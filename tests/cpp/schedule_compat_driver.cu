@@ -156,7 +156,7 @@ int main(int argc, char** argv) {
   if (n) CHECK(cudaMemcpy(d_z, ones.data(), n * 4, cudaMemcpyHostToDevice));
 
   constexpr std::size_t tpb = 128;
-  const unsigned row_blocks = (unsigned)((rows + tpb - 1) / tpb);
+  const unsigned row_blocks = (unsigned)math::ceil_div((std::size_t)rows, tpb);
   if (rows > 0) {
     // a small grid, so that threads take several rows / a long share each
     spmv_thread_mapped<int, int, float><<<7, tpb>>>(rows, cols, nnz, d_off, d_idx, d_val, d_x,
@@ -165,8 +165,9 @@ int main(int argc, char** argv) {
                                                          d_x, d_y2);
     spmv_warp_mapped<tpb, int, int, float><<<row_blocks, tpb>>>(rows, cols, nnz, d_off, d_idx,
                                                                 d_val, d_x, d_y3);
-    spmv_block_mapped<tpb, int, int, float><<<row_blocks, tpb>>>(rows, cols, nnz, d_off, d_idx,
-                                                                 d_val, d_x, d_y4, d_vis);
+    launch::non_cooperative(nullptr, spmv_block_mapped<tpb, int, int, float>, row_blocks, tpb,
+                            (std::size_t)rows, (std::size_t)cols, (std::size_t)nnz, d_off, d_idx,
+                            (const float*)d_val, (const float*)d_x, d_y4, d_vis);
   }
   if (n) saxpy<<<3, 64>>>((int)n, 2.0f, d_x, d_z);
   CHECK(cudaGetLastError());

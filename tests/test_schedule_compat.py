@@ -34,6 +34,7 @@ def test_same_driver_compiles_against_the_reference_headers(tmp_path):
     shim.mkdir()
     (shim / "edge_loops_schedule.cuh").write_text(
         "#pragma once\n#include <thrust/device_vector.h>\n#include <loops/error.hxx>\n"
+        "#include <loops/util/math.hxx>\n#include <loops/util/launch.hxx>\n"
         "#include <loops/stride_ranges.hxx>\n#include <loops/schedule.hxx>\n")
     subprocess.run([NVCC] + ARCH + ["-std=c++17", "--expt-extended-lambda",
                                     "--expt-relaxed-constexpr", "-w", "-c",
