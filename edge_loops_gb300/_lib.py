@@ -188,6 +188,7 @@ SIGNATURES = {
                                      C.POINTER(C.c_double)]),
     "el_spmv_select": (C.c_int, [C.c_void_p, C.POINTER(ElCsr), C.POINTER(C.c_int32),
                                  C.POINTER(ElSpmvOpts), C.c_void_p]),
+    "el_debug_range_trace": (C.c_int, [C.c_void_p, C.c_int64]),
     "el_spmv_edge": (C.c_int, [C.c_void_p, C.POINTER(ElCoo), C.POINTER(ElEdgePartition),
                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 }

@@ -28,6 +28,8 @@ namespace el {
 
 namespace {
 thread_local std::string g_last_error;
+thread_local long long* g_trace = nullptr;  // el_debug_range_trace
+thread_local long long g_trace_cap = 0;
 std::mutex g_mu;
 std::map<std::pair<int, cudaStream_t>, el_workspace*> g_default_ws;
 std::map<int, DeviceInfo> g_dev_info;
@@ -52,6 +54,11 @@ el_status cuda_status(cudaError_t e, const char* what) {
   if (e == cudaErrorMemoryAllocation)
     return fail(EL_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
   return fail(EL_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+void range_trace(long long** buf, long long* cap) {
+  *buf = g_trace;
+  *cap = g_trace ? g_trace_cap : 0;
 }
 
 const DeviceInfo& device_info(int device) {
@@ -276,6 +283,13 @@ const char* el_status_string(el_status s) {
 
 const char* el_last_error_string(void) { return g_last_error.c_str(); }
 
+el_status el_debug_range_trace(int64_t* ranges, int64_t capacity) {
+  if (ranges && capacity <= 0) return fail(EL_ERR_INVALID_ARGUMENT, "capacity must be > 0");
+  g_trace = reinterpret_cast<long long*>(ranges);
+  g_trace_cap = ranges ? capacity : 0;
+  return EL_OK;
+}
+
 void el_spmv_opts_default(el_spmv_opts* o) {
   if (!o) return;
   std::memset(o, 0, sizeof(*o));
@@ -353,6 +367,7 @@ el_status el_spmv(el_workspace* ws, const el_csr* A, int32_t schedule,
   c.stream = (cudaStream_t)stream;
   c.wait_ns = c.o.wait_limit_us > 0 ? (unsigned long long)c.o.wait_limit_us * 1000ull
                                      : kDefaultWaitNs;
+  range_trace(&c.trace, &c.trace_cap);
   cudaError_t e = cudaGetDevice(&c.device);
   if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
   if (A->rows == 0) return EL_OK;

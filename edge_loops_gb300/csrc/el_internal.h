@@ -40,6 +40,8 @@ struct SpmvCall {
   cudaStream_t stream;
   uint64_t wait_ns;
   int device;
+  long long* trace = nullptr;  // el_debug_range_trace buffer (testing only)
+  long long trace_cap = 0;     // ranges it holds
 };
 
 struct SpmmCall {
@@ -78,6 +80,10 @@ el_status launch_work_oriented(const SpmvCall& c);
 el_status launch_spmm(const SpmmCall& c, int schedule);
 size_t spmm_scratch_bytes(const SpmmCall& c, int schedule);
 long long spmm_slots_needed(const SpmmCall& c, int schedule);
+
+// The range-trace buffer that el_debug_range_trace set on this host thread
+// (nullptr and 0 when none).
+void range_trace(long long** buf, long long* cap);
 
 // Workspace internals for other translation units of the library.
 WsView workspace_view(el_workspace* ws);

@@ -53,6 +53,8 @@ struct Args {
   int test_hooks;
   unsigned long long wait_ns;
   WsView ws;
+  long long* trace;       // testing only: per range (d0, d1, rs, ns, re, ne), or nullptr
+  long long trace_cap;    // ranges the trace holds
 };
 
 template <bool COMP>
@@ -543,6 +545,15 @@ __device__ __forceinline__ void run_range(const Args& a, SmemT& S, const int war
     const int ne = nz_of(d1, sb);
     const int off_rs = sa.start;
     const bool need_lb = ns > off_rs;
+    if (a.trace && g < a.trace_cap && lane < 6) {
+      // the range's diagonals and split points exactly as the walk uses them
+      const long long t6[6] = {d0, d1, rs, ns, re, ne};
+      long long tv = t6[0];
+#pragma unroll
+      for (int k = 1; k < 6; ++k)
+        if (lane == k) tv = t6[k];
+      a.trace[6 * g + lane] = tv;
+    }
     if (lane == 0) {
       S.pend = 0;
       if (g == 0 && off_rs != 0) raise_flag(hdr, EL_FLAG_NNZ_MISMATCH, 0);
@@ -674,6 +685,8 @@ el_status launch(const SpmvCall& c) {
   a.test_hooks = c.o.test_hooks;
   a.wait_ns = c.wait_ns;
   a.ws = c.ws;
+  a.trace = c.trace;
+  a.trace_cap = c.trace_cap;
   if (a.num_ranges > c.ws.nslots)
     return fail(EL_ERR_INVALID_ARGUMENT, "merge_path: workspace too small");
   const long long grid = (a.num_ranges + kWarps - 1) / kWarps;

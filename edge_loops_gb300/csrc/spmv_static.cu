@@ -70,6 +70,7 @@ el_status launch_static(const el_csr& A, const float* x, float* y, int ranges, v
   a.ws.hdr = reinterpret_cast<WsHeader*>(scratch);
   a.ws.slots = reinterpret_cast<CarrySlot*>(reinterpret_cast<char*>(scratch) + sizeof(WsHeader));
   a.ws.nslots = kStaticRanges;
+  range_trace(&a.trace, &a.trace_cap);
   const long long grid = (a.num_ranges + kWarps - 1) / kWarps;
   merge_path_nz_kernel<VT, false><<<(unsigned)grid, kTPB, 0, stream>>>(a);
   return cuda_status(cudaGetLastError(), "static-scratch merge_path launch");

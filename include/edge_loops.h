@@ -399,6 +399,18 @@ el_status el_work_oriented_partition(const int32_t* offsets, int64_t rows,
                                      int64_t nnz, int64_t num_threads,
                                      int64_t* coords, el_stream_t stream);
 
+/* Testing only (no counterpart in the reference): while `ranges` is not
+ * NULL, every launch of the default merge-path kernel (el_spmv with
+ * EL_SCHED_MERGE_PATH_FLAT and variant 0, el_spmv_static_scratch) made from
+ * the calling host thread writes, for each of its warp ranges g < capacity,
+ * six int64 to ranges[6 g .. 6 g + 5]: the range's first and end merge
+ * diagonal, then the (row, nonzero) coordinates the kernel itself computed
+ * for them -- first row, first nonzero, end row, end nonzero.  With a row
+ * weight of 1 these are the reference's merge-path split points
+ * (util/search.hxx:34-60) at those diagonals.  `ranges` is device memory of
+ * 6 * capacity int64; NULL switches the trace off. */
+el_status el_debug_range_trace(int64_t* ranges, int64_t capacity);
+
 /* ---- batched SpMV (no counterpart in the reference) --------------------
  * Thousands of independent CSR matrices, each with its own x and y, run in
  * ONE persistent launch that the plan captures in a CUDA graph.  A plan

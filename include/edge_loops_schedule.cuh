@@ -5,7 +5,8 @@
 // A kernel written against the reference's load-balancing API
 // (docs/loadbalancing_api.md; include/loops/schedule.hxx:21-46,
 // stride_ranges.hxx:16-64, schedule/thread_mapped.hxx:88-166,
-// schedule/work_oriented.hxx:86-195, schedule/group_mapped.hxx:80-250)
+// schedule/work_oriented.hxx:86-195, schedule/group_mapped.hxx:80-250,
+// schedule/merge_path_flat.hxx:158-436)
 // compiles against this header unchanged (it also replaces
 // <loops/util/math.hxx> and <loops/util/launch.hxx>: math::ceil_div,
 // launch::non_cooperative, launch::cooperative):
@@ -45,11 +46,31 @@
 // w = ceil((rows + nnz) / (gridDim.x * threads_per_block)), complete rows
 // first, then the part of the row still open at its end; group_mapped gives
 // each group of threads_per_tile threads the rows of its threads (one row
-// per thread of the grid) and strides the group over their nonzeros.  The
-// merge_path_flat setup is not offered: its loop body reads the setup's
-// shared-memory tile state directly; edge_loops_device.cuh has the
-// merge-path split points and range walk for such kernels.  Ranges here
-// step forward only.
+// per thread of the grid) and strides the group over their nonzeros;
+// merge_path_flat cuts the merge of row ends and nonzeros into blocks of
+// threads_per_block * items_per_thread items at diagonals k * that size and
+// gives each thread items_per_thread consecutive items from diagonal
+// threadIdx.x * items_per_thread of its block's tile:
+//
+//   using setup_t = loops::schedule::setup<loops::schedule::algorithms_t::merge_path_flat,
+//                                          threads_per_block, items_per_thread, index_t,
+//                                          offset_t, std::size_t, std::size_t>;
+//   // host: typename setup_t::meta_t meta(offsets, rows, nnz, stream);
+//   __shared__ typename setup_t::storage_t storage;
+//   setup_t config(meta, storage, offsets, rows, nnz);
+//   auto map = config.init();                    // every thread of the block
+//   if (!config.is_valid_accessor(map)) return;
+//   for (auto item : config.virtual_idx()) {
+//     auto nz = config.atom_idx(item, map);      // clamped to nnz - 1
+//     auto row = config.tile_idx(map);
+//     if (config.atoms_counting_it[map.y] < storage.tile_end_offset[map.x]) {
+//       ... nonzero nz of row `row` ...; map.y++;
+//     } else {
+//       map.x++;                                 // row `row` ends here
+//     }
+//   }
+//
+// Ranges here step forward only.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -171,7 +192,26 @@ cudaError_t cooperative(cudaStream_t stream, const func_t& kernel, std::size_t n
 }
 }  // namespace launch
 
+// A (row, nonzero) point of the merge path (the reference's
+// coordinate_t, container/coordinate.hxx).
+template <typename index_t>
+struct coordinate_t {
+  index_t x;
+  index_t y;
+};
+
+// i -> begin + i, as the reference's thrust::counting_iterator is used by
+// merge-path loop bodies (it[i], *it).
+template <typename T>
+struct counting_t {
+  T base;
+  __host__ __device__ T operator[](long long i) const { return T((long long)base + i); }
+  __host__ __device__ T operator*() const { return base; }
+};
+
 namespace schedule {
+
+using coord_t = coordinate_t<unsigned int>;
 
 enum algorithms_t {
   merge_path_flat,
@@ -184,7 +224,177 @@ enum algorithms_t {
 template <algorithms_t scheme, std::size_t threads_per_block, std::size_t threads_per_tile,
           typename tiles_t, typename atoms_t, typename tile_size_t = std::size_t,
           typename atom_size_t = std::size_t>
-class setup;  // thread_mapped, work_oriented and group_mapped are defined below
+class setup;  // every schedule but bucketing is defined below
+
+// ---------------------------------------------------------- merge_path_flat
+namespace merge_path {
+
+// The merge-path point of diagonal `diag` of the merge of list a (row ends,
+// a_len of them) with the counting list b0, b0 + 1, ... (b_len nonzeros):
+// x = the first index in [max(diag - b_len, 0), min(diag, a_len)) where
+// a[x] <= b0 + diag - x - 1 fails (the start of the interval when it is
+// empty or inverted), point (min(x, a_len), diag - x).  This is the
+// reference's search::_binary_search (util/search.hxx:34-60); the failing
+// index is unique, so this bisection finds the same point.
+template <typename A>
+__device__ __forceinline__ coord_t point(long long diag, const A& a, long long a_len,
+                                         long long b0, long long b_len) {
+  long long lo = diag - b_len > 0 ? diag - b_len : 0;
+  long long hi = diag < a_len ? diag : a_len;
+  while (lo < hi) {
+    const long long mid = lo + ((hi - lo) >> 1);
+    if ((long long)a[mid] <= b0 + diag - mid - 1)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return coord_t{(unsigned int)(lo < a_len ? lo : a_len), (unsigned int)(diag - lo)};
+}
+
+// The reference's preprocess object (schedule/merge_path_flat.hxx:158-230),
+// passed to the kernel by value.  The reference may compute every block's
+// start point in a separate launch, but its copy constructor leaves the
+// kernel's copy without them, so its kernels always search themselves.
+// Here nothing is computed or allocated; a caller that has the points
+// (el_merge_path_partition writes them: 2 x (tiles + 1) unsigned int) may
+// pass them as `tile_coords`, and the blocks then read their start and end
+// points from there.
+template <std::size_t THREADS_PER_BLOCK, std::size_t ITEMS_PER_THREAD, typename tiles_type,
+          typename atoms_type, typename tile_size_type, typename atom_size_type>
+class preprocess_t {
+ public:
+  using tiles_t = tiles_type;
+  using atoms_t = atoms_type;
+  using tiles_iterator_t = tiles_t*;
+  using tile_size_t = tile_size_type;
+  using atom_size_t = atom_size_type;
+
+  __host__ preprocess_t(tiles_iterator_t, tile_size_t, atom_size_t, cudaStream_t = 0,
+                        coord_t* tile_coords = nullptr)
+      : coords_(tile_coords) {}
+  __host__ __device__ coord_t* data() const { return coords_; }
+
+ private:
+  coord_t* coords_;
+};
+
+}  // namespace merge_path
+
+template <std::size_t THREADS_PER_BLOCK, std::size_t ITEMS_PER_THREAD, typename tiles_type,
+          typename atoms_type, typename tile_size_type, typename atom_size_type>
+class setup<algorithms_t::merge_path_flat, THREADS_PER_BLOCK, ITEMS_PER_THREAD, tiles_type,
+            atoms_type, tile_size_type, atom_size_type> {
+ public:
+  using tiles_t = tiles_type;
+  using atoms_t = atoms_type;
+  using tiles_iterator_t = tiles_t*;
+  using atoms_iterator_t = atoms_t*;
+  using tile_size_t = tile_size_type;
+  using atom_size_t = atom_size_type;
+  using meta_t = merge_path::preprocess_t<THREADS_PER_BLOCK, ITEMS_PER_THREAD, tiles_type,
+                                          atoms_type, tile_size_type, atom_size_type>;
+
+  enum : unsigned int {
+    threads_per_block = THREADS_PER_BLOCK,
+    items_per_thread = ITEMS_PER_THREAD,
+    items_per_tile = THREADS_PER_BLOCK * ITEMS_PER_THREAD,
+  };
+
+  // Shared state of one block (declare it __shared__ in the kernel): the
+  // block's start and end points, and the ends of the rows its tile touches
+  // (entry i = end of row start.x + i, the last row's end past the tile) --
+  // the loop body compares nonzero indices with them.
+  struct storage_t {
+    coord_t tile_coords[2];
+    tiles_t tile_end_offset[items_per_thread + items_per_tile + 1];
+  };
+
+  storage_t& buffer;
+  meta_t& meta;
+  counting_t<atoms_t> atoms_counting_it;  // tile-local nonzero -> nonzero index
+  counting_t<tiles_t> tiles_counting_it;  // tile-local row -> row index
+
+  __device__ __forceinline__ setup(meta_t& _meta, storage_t& _buffer, tiles_iterator_t tiles,
+                                   tile_size_t num_tiles, atom_size_t num_atoms)
+      : buffer(_buffer),
+        meta(_meta),
+        atoms_counting_it{atoms_t(0)},
+        tiles_counting_it{tiles_t(0)},
+        tiles_(tiles),
+        num_tiles_(num_tiles),
+        num_atoms_(num_atoms),
+        num_merge_tiles_(((std::size_t)num_tiles + (std::size_t)num_atoms + items_per_tile - 1) /
+                         items_per_tile),
+        tile_num_tiles_(0),
+        tile_num_atoms_(0) {}
+
+  // Every thread of the block calls this.  Block b (b = blockIdx.x *
+  // gridDim.y + blockIdx.y) owns diagonals [b T, (b + 1) T), T =
+  // items_per_tile; the thread's point is the tile-local merge-path point of
+  // diagonal threadIdx.x * items_per_thread.  Blocks past the last tile get
+  // an invalid point (both coordinates all ones).
+  __device__ __forceinline__ coord_t init() {
+    const std::size_t b = (std::size_t)blockIdx.x * gridDim.y + blockIdx.y;
+    if (b >= num_merge_tiles_) return coord_t{~0u, ~0u};
+    const long long rows = (long long)num_tiles_, nnz = (long long)num_atoms_;
+    if (threadIdx.x < 2) {
+      const coord_t* pre = meta.data();
+      buffer.tile_coords[threadIdx.x] =
+          pre ? pre[b + threadIdx.x]
+              : merge_path::point((long long)(b + threadIdx.x) * items_per_tile, tiles_ + 1,
+                                  rows, 0, nnz);
+    }
+    __syncthreads();
+    const coord_t st = buffer.tile_coords[0], en = buffer.tile_coords[1];
+    tile_num_tiles_ = tile_size_t(en.x - st.x);
+    tile_num_atoms_ = atom_size_t(en.y - st.y);
+    const long long last = rows - 1;
+    for (long long i = threadIdx.x; i < (long long)tile_num_tiles_ + items_per_thread;
+         i += threads_per_block) {
+      const long long r = (long long)st.x + i < last ? (long long)st.x + i : last;
+      buffer.tile_end_offset[i] = tiles_[r + 1];
+    }
+    atoms_counting_it = counting_t<atoms_t>{atoms_t(st.y)};
+    tiles_counting_it = counting_t<tiles_t>{tiles_t(st.x)};
+    __syncthreads();
+    const coord_t mine = merge_path::point((long long)threadIdx.x * items_per_thread,
+                                           buffer.tile_end_offset, (long long)tile_num_tiles_,
+                                           (long long)st.y, (long long)tile_num_atoms_);
+    __syncthreads();  // the tile state is read-only from here on
+    return mine;
+  }
+
+  __device__ __forceinline__ bool is_valid_accessor(coord_t& c) const {
+    return c.x != ~0u && c.y != ~0u;
+  }
+  // the thread's items 0 .. items_per_thread - 1
+  __device__ __forceinline__ step_range_t<int> virtual_idx() const {
+    return custom_stride_range(int(0), int(items_per_thread), int(1));
+  }
+  // The nonzero index at the point (not advanced), clamped to the last
+  // nonzero as the reference clamps it (merge_path_flat.hxx:408-410), so an
+  // item that is a row end still reads a valid nonzero.  With no nonzeros
+  // at all this is -1, as in the reference: such a matrix has no item to
+  // read.
+  __device__ __forceinline__ atoms_t atom_idx(int, coord_t& c) const {
+    const long long nz = (long long)atoms_counting_it[c.y];
+    const long long last = (long long)num_atoms_ - 1;
+    return atoms_t(nz < last ? nz : last);
+  }
+  // the row index at the point (not advanced)
+  __device__ __forceinline__ tiles_t tile_idx(coord_t& c) const { return tiles_counting_it[c.x]; }
+  // rows ending in, and nonzeros of, this block's tile
+  __device__ __forceinline__ tile_size_t num_tiles() const { return tile_num_tiles_; }
+  __device__ __forceinline__ atom_size_t num_atoms() const { return tile_num_atoms_; }
+
+ private:
+  tiles_iterator_t tiles_;
+  tile_size_t num_tiles_;
+  atom_size_t num_atoms_;
+  std::size_t num_merge_tiles_;
+  tile_size_t tile_num_tiles_;
+  atom_size_t tile_num_atoms_;
+};
 
 // ---------------------------------------------------------- thread_mapped
 template <typename tiles_type, typename atoms_type, typename tile_size_type,

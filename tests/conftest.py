@@ -69,3 +69,34 @@ def order_free_bound(offsets, yabs, extra=2):
     u = 2.0 ** -24
     n = np.diff(offsets.astype(np.int64)) + extra
     return (n * u / (1 - n * u)) * yabs
+
+
+def merge_coords_weighted(off, d, w):
+    """Coordinates at diagonals d of the merge with every row end counted as w
+    items (closed form)."""
+    off = off.astype(np.int64)
+    rows = len(off) - 1
+    ends = off[1:] + w * np.arange(1, rows + 1, dtype=np.int64)
+    x = np.searchsorted(ends, d, side="right")
+    n = d - w * x
+    lim = np.where(x < rows, off[np.minimum(x + 1, rows)], np.iinfo(np.int64).max)
+    return x, np.minimum(n, lim)
+
+
+def merge_walk_weighted(off, w):
+    """Item-by-item walk of the weighted merge: the (row, nonzero) state after
+    each number of items 0..w rows + nnz (a row end is w items; the row
+    closes on its last one)."""
+    rows = len(off) - 1
+    r = n = 0
+    out = [(0, 0)]
+    pend = 0  # items of the current row end consumed so far
+    while r < rows or n < off[-1]:
+        if r < rows and n == off[r + 1]:
+            pend += 1
+            if pend == w:
+                r, pend = r + 1, 0
+        else:
+            n += 1
+        out.append((r, n))
+    return np.array(out, dtype=np.int64)

@@ -11,6 +11,11 @@
 //        float y_block[rows]   (block_mapped setup, atomics)
 //        int32 visits[nnz]     (block_mapped: times each nonzero was visited)
 //        float z[n]            (2 x + z0 by grid_stride_range, z0 = 1)
+//        float y_merge[rows]   (merge_path_flat setup, 128 x 5 items per
+//                               block, atomics, as the reference's kernel)
+//        uint32 coords[tiles * 128 * 2]  (each thread's tile-local start
+//                               point from init(); tiles = ceil((rows +
+//                               nnz) / 640); skipped when nnz == 0)
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -100,6 +105,34 @@ __global__ void spmv_block_mapped(std::size_t rows, std::size_t cols, std::size_
   group_body<setup_t>(storage, rows, nnz, offsets, indices, values, x, y, visits);
 }
 
+template <std::size_t threads_per_block, std::size_t items_per_thread, typename meta_t,
+          typename index_t, typename offset_t, typename type_t>
+__global__ void spmv_merge_path(meta_t meta, std::size_t rows, std::size_t cols, std::size_t nnz,
+                                offset_t* offsets, index_t* indices, const type_t* values,
+                                const type_t* x, type_t* y, unsigned* coords) {
+  using setup_t = schedule::setup<schedule::algorithms_t::merge_path_flat, threads_per_block,
+                                  items_per_thread, index_t, offset_t, std::size_t,
+                                  std::size_t>;
+  __shared__ typename setup_t::storage_t storage;
+  setup_t config(meta, storage, offsets, rows, nnz);
+  auto map = config.init();
+  if (!config.is_valid_accessor(map)) return;
+  const std::size_t t = (std::size_t)blockIdx.x * threads_per_block + threadIdx.x;
+  coords[2 * t] = map.x;
+  coords[2 * t + 1] = map.y;
+  for (auto item : config.virtual_idx()) {
+    auto nz = config.atom_idx(item, map);
+    auto row = config.tile_idx(map);
+    type_t nonzero = values[nz] * x[indices[nz]];
+    if (config.atoms_counting_it[map.y] < storage.tile_end_offset[map.x]) {
+      atomicAdd(&(y[row]), nonzero);
+      map.y++;
+    } else {
+      map.x++;
+    }
+  }
+}
+
 template <typename T>
 static T* upload(const std::vector<T>& h) {
   T* d = nullptr;
@@ -170,6 +203,22 @@ int main(int argc, char** argv) {
                             (const float*)d_val, (const float*)d_x, d_y4, d_vis);
   }
   if (n) saxpy<<<3, 64>>>((int)n, 2.0f, d_x, d_z);
+  // merge_path_flat: one block per tile of 128 x 5 merge items
+  constexpr std::size_t ipt = 5;
+  const std::size_t tiles = math::ceil_div((std::size_t)(rows + nnz), tpb * ipt);
+  float* d_y5;
+  unsigned* d_coords;
+  CHECK(cudaMalloc(&d_y5, ry * 4));
+  CHECK(cudaMemset(d_y5, 0, ry * 4));
+  CHECK(cudaMalloc(&d_coords, (tiles > 0 ? tiles : 1) * tpb * 2 * 4));
+  CHECK(cudaMemset(d_coords, 0xff, (tiles > 0 ? tiles : 1) * tpb * 2 * 4));
+  if (rows > 0 && nnz > 0) {
+    using meta_t = schedule::merge_path::preprocess_t<tpb, ipt, int, int, std::size_t,
+                                                      std::size_t>;
+    meta_t meta(d_off, (std::size_t)rows, (std::size_t)nnz);
+    spmv_merge_path<tpb, ipt, meta_t, int, int, float><<<(unsigned)tiles, tpb>>>(
+        meta, rows, cols, nnz, d_off, d_idx, d_val, d_x, d_y5, d_coords);
+  }
   CHECK(cudaGetLastError());
   CHECK(cudaDeviceSynchronize());
 
@@ -184,6 +233,10 @@ int main(int argc, char** argv) {
   put(vis.data(), vis.size() * 4);
   auto z = download(d_z, (size_t)n);
   put(z.data(), z.size() * 4);
+  auto y5 = download(d_y5, (size_t)rows);
+  put(y5.data(), y5.size() * 4);
+  auto co = download(d_coords, nnz > 0 ? tiles * tpb * 2 : 0);
+  put(co.data(), co.size() * 4);
   std::fclose(o);
   return 0;
 }

@@ -5,7 +5,7 @@ walk.  CPU only."""
 import numpy as np
 import pytest
 
-from conftest import load_golden, random_csr
+from conftest import load_golden, merge_coords_weighted, merge_walk_weighted, random_csr
 
 
 def test_chesapeake_matches_reference_fixture(oracle_mod):
@@ -180,3 +180,23 @@ def test_split_points_property_random_shapes(oracle_mod):
             assert tuple(c[t, 2:]) == tuple(walk[min(up + wpt, total)])
 
     check()
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_weighted_merge_closed_form(oracle_mod, seed):
+    """The closed form the GPU split-point test holds the kernel's weighted
+    ranges to: equal to an item-by-item walk for row weights 1-3, and for
+    weight 1 to the restated reference search (util/search.hxx:34-60)."""
+    rng = np.random.default_rng(seed)
+    rows = int(rng.integers(1, 60))
+    off, _, _, _ = random_csr(rng, rows, 50, max_len=int(rng.integers(0, 12)),
+                              empty_frac=float(rng.choice([0.0, 0.5])))
+    nnz = int(off[-1])
+    for w in (1, 2, 3):
+        walk = merge_walk_weighted(off, w)
+        d = np.arange(w * rows + nnz + 1, dtype=np.int64)
+        x, n = merge_coords_weighted(off, d, w)
+        np.testing.assert_array_equal(np.stack([x, n], 1), walk)
+        if w == 1:
+            for k in d:
+                assert oracle_mod.mp_search(int(k), off[1:], rows, 0, nnz) == tuple(walk[k])
