@@ -134,6 +134,56 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# ------------------------------------------------------------- FP64 checker
+# The benchmark checks its own outputs with this plain FP64 evaluation
+# (numpy, row blocks of a few million nonzeros); the CPU oracle package is
+# used only by the CPU-baseline and reference legs.
+def fp64_spmv(off, idx, vals, x, scale=None, chunk=1 << 24):
+    """(y, sum_j |a_ij x_j|) in FP64 for a host CSR; vals any float dtype
+    (16-bit values given as their float32 widening), scale per row or None."""
+    import numpy as np
+    off = np.asarray(off, dtype=np.int64)
+    rows = len(off) - 1
+    x64 = np.asarray(x, dtype=np.float64)
+    y = np.zeros(rows)
+    ya = np.zeros(rows)
+    r0 = 0
+    while r0 < rows:
+        r1 = int(np.searchsorted(off, off[r0] + chunk, side="right")) - 1
+        r1 = min(max(r1, r0 + 1), rows)
+        n0, n1 = int(off[r0]), int(off[r1])
+        row_of = np.repeat(np.arange(r1 - r0), np.diff(off[r0:r1 + 1]))
+        prod = np.asarray(vals[n0:n1], dtype=np.float64) * x64[np.asarray(idx[n0:n1])]
+        y[r0:r1] = np.bincount(row_of, prod, minlength=r1 - r0)
+        ya[r0:r1] = np.bincount(row_of, np.abs(prod), minlength=r1 - r0)
+        r0 = r1
+    if scale is not None:
+        sc = np.asarray(scale, dtype=np.float64)
+        y *= sc
+        ya *= np.abs(sc)
+    return y, ya
+
+
+def fp32_bound(off, yabs, extra=2):
+    """|fp32 sum - exact| <= gamma_(n+extra) * sum |a x| for any summation
+    order of a row's n products (each rounded once)."""
+    import numpy as np
+    u = 2.0 ** -24
+    n = np.diff(np.asarray(off, dtype=np.int64)) + extra
+    return (n * u / (1 - n * u)) * yabs
+
+
+def rel_errors(y, y64, yabs):
+    """(max_i |y_i - y64_i| / sum_j |a_ij x_j|, ||y - y64||_inf / ||y64||_inf)."""
+    import numpy as np
+    d = np.abs(np.asarray(y, dtype=np.float64) - y64)
+    if not len(d):
+        return 0.0, 0.0
+    comp = float(np.max(d / np.where(yabs > 0, yabs, 1.0)))
+    ninf = float(np.max(np.abs(y64)))
+    return comp, float(np.max(d) / ninf) if ninf > 0 else float(np.max(d))
+
+
 # ------------------------------------------------------------------ workloads
 def make_workload(name, device, value_dtype):
     """Returns dict(off, idx, vals, x, rows, cols, desc) on `device` (FP32
@@ -284,7 +334,76 @@ def run_ours(args, rank, world):
     }
     if rank == 0 and args.cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(W, args, budget_s=args.cpu_budget)
+    if rank == 0 and args.secondary and args.workload == "spmv_powerlaw" and \
+            args.schedule == "merge_path_flat" and args.value_dtype == "f32" and not args.variant:
+        del A, x, y, W
+        torch.cuda.empty_cache()
+        line["secondary"] = run_secondary(args, dev)
     return line
+
+
+def run_secondary(args, dev):
+    """The other configurations of the target, measured in the same run as
+    the headline (same timing rules: L2 flushed before every step, outside
+    the CUDA events): the 27-point stencil on 160^3 with FP32, BF16 and FP16
+    values (16-bit with per-row scales), and the 4096-matrix batch
+    (measure_batched: BF16 and FP32 plans and the plain FP32 kernel once per
+    matrix).  Every output is checked against FP64."""
+    import numpy as np
+    import torch
+    from edge_loops_gb300 import api, synth
+    peak, kind = measured_peaks()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, device=dev)
+    stream = torch.cuda.current_stream()
+    steps = max(5, min(args.steps, 20))
+    warm = max(3, min(args.warmup, 5))
+    out = {"steps": steps, "warmup": warm, "peak_GBps": peak, "peak_source": kind}
+
+    off, idx, vals, x, rows = synth.stencil27(n=160, seed=2, device=dev)
+    A = api.CSR(off, idx, vals, rows, rows)
+    o, i, v, xh = (t.cpu().numpy() for t in (off, idx, vals, x))
+    y64, yabs = fp64_spmv(o, i, v, xh)
+    ws = api.Workspace()
+    st = {"workload": "27-point stencil on 160^3 (4,096,000 rows, 109,215,352 nnz), diag 26.5, "
+                      "off-diag U[-1,0], x U[-1,1], seed 2; merge_path"}
+    for dt in ("f32", "bf16", "f16"):
+        Q = A if dt == "f32" else A.quantized(
+            torch.bfloat16 if dt == "bf16" else torch.float16, per_row_scale=True)
+        y = torch.empty(rows, device=dev)
+        ms = _time_device(lambda: api.spmv(Q, x, y, workspace=ws), steps, warm, flush, stream)
+        if ws.errors():
+            raise SystemExit(f"device error flags in the stencil {dt} SpMV")
+        nb = synth.algorithmic_bytes(rows, rows, Q.nnz, 4 if dt == "f32" else 2,
+                                     row_scale=Q.row_scale is not None)
+        yy = y.cpu().numpy()
+        if dt == "f32":
+            bad = int(np.sum(np.abs(yy - y64) > fp32_bound(o, yabs)))
+        else:
+            q64, qabs = fp64_spmv(o, i, Q.values.float().cpu().numpy(), xh,
+                                  Q.row_scale.cpu().numpy())
+            bad = int(np.sum(np.abs(yy - q64) > fp32_bound(o, qabs)))
+        comp, _ = rel_errors(yy, y64, yabs)
+        if bad or comp > 1e-2:
+            raise SystemExit(f"stencil {dt}: {bad} rows outside the FP32 bound, err {comp}")
+        gbps = nb / (ms * 1e-3) / 1e9
+        st[dt] = {"us": round(ms * 1e3, 2), "GBps": round(gbps, 1), "frac": round(gbps / peak, 4),
+                  "algorithmic_bytes": nb, "rows_outside_fp32_bound": bad,
+                  "max_rel_err_vs_fp64_of_fp32_matrix": comp}
+        del Q, y
+    for dt in ("bf16", "f16"):
+        st[dt]["time_vs_f32"] = round(st[dt]["us"] / st["f32"]["us"], 4)
+    out["stencil160"] = st
+    del A, off, idx, vals, x, ws
+    torch.cuda.empty_cache()
+
+    b = measure_batched(dev, steps, warm, flush, stream, ("bf16",))
+    b["workload"] = ("4096 square CSRs, rows log-uniform [64, 65536], log-normal nnz/row "
+                     "(mean 8, sigma 1), seed 4; one persistent launch per plan in a CUDA graph")
+    for dt in ("f32", "bf16"):
+        b[dt]["frac"] = round(b[dt]["GBps"] / peak, 4)
+    out["batched4096"] = b
+    torch.cuda.empty_cache()
+    return out
 
 
 def graph_replay(step, stream, nbytes, reps=100, runs=5):
@@ -316,10 +435,10 @@ def graph_replay(step, stream, nbytes, reps=100, runs=5):
 
 
 def verify(args, A, x, y, W):
-    """Parity of the benchmarked output: the oracle on the same input, in full
-    (the CPU loop finishes in about a second at these sizes)."""
+    """Parity of the benchmarked output: FP64 on the same input, every row,
+    within the order-free FP32 bound (of the stored values for 16-bit runs)
+    and, for 16-bit values, the error against FP64 of the FP32 matrix."""
     import numpy as np
-    import oracle
     off = W["off"].cpu().numpy()
     idx = W["idx"].cpu().numpy()
     xx = x.cpu().numpy()
@@ -330,21 +449,18 @@ def verify(args, A, x, y, W):
     else:
         vals = A.values.float().cpu().numpy()
         scale = A.row_scale.cpu().numpy() if A.row_scale is not None else None
-    y64, yabs = oracle.spmv_f64(off, idx, vals, xx, row_scale=scale)
-    u = 2.0 ** -24
-    n = np.diff(off.astype(np.int64)) + 2
-    bound = (n * u / (1 - n * u)) * yabs
-    bad = int(np.sum(np.abs(yy - y64) > bound))
-    comp, norm = oracle.error_metrics(yy, y64, yabs)
+    y64, yabs = fp64_spmv(off, idx, vals, xx, scale)
+    bad = int(np.sum(np.abs(yy - y64) > fp32_bound(off, yabs)))
+    comp, norm = rel_errors(yy, y64, yabs)
     out = {"rows_outside_fp32_bound": bad, "max_rel_err_vs_fp64_stored": comp,
            "normwise_err_vs_fp64_stored": norm}
     if args.value_dtype != "f32":
-        y64o, yabso = oracle.spmv_f64(off, idx, W["vals"].cpu().numpy(), xx)
-        c2, n2 = oracle.error_metrics(yy, y64o, yabso)
+        y64o, yabso = fp64_spmv(off, idx, W["vals"].cpu().numpy(), xx)
+        c2, n2 = rel_errors(yy, y64o, yabso)
         out["max_rel_err_vs_fp64_fp32matrix"] = c2
         out["normwise_err_vs_fp64_fp32matrix"] = n2
     if bad:
-        raise SystemExit(f"benchmarked y fails the oracle check: {out}")
+        raise SystemExit(f"benchmarked y fails the FP64 check: {out}")
     return out
 
 
@@ -358,7 +474,6 @@ def run_e2e(args, A, W, nbytes, dev, world=1):
     time counts, and value and bytes are the whole job's."""
     import numpy as np
     import torch
-    import oracle
     from edge_loops_gb300 import api
     h_off = A.offsets.cpu().pin_memory()
     h_idx = A.indices.cpu().pin_memory()
@@ -419,17 +534,15 @@ def run_e2e(args, A, W, nbytes, dev, world=1):
 
     ms_copy, _ = timed(step_copy)
     ms, steps = timed(step_stream)
-    # the streamed y against the FP64 oracle (block borders change the merge
-    # ranges, so the check is the FP32 bound, not equality)
+    # the streamed y against FP64 (block borders change the merge ranges, so
+    # the check is the FP32 bound, not equality)
     off = W["off"].cpu().numpy()
     vals = A.values.float().cpu().numpy()
-    y64, yabs = oracle.spmv_f64(off, W["idx"].cpu().numpy(), vals, W["x"].cpu().numpy(),
-                                row_scale=None if h_sc is None else h_sc.numpy())
-    u = 2.0 ** -24
-    n = np.diff(off.astype(np.int64)) + 2
-    bad = int(np.sum(np.abs(h_y.numpy().astype(np.float64) - y64) > (n * u / (1 - n * u)) * yabs))
+    y64, yabs = fp64_spmv(off, W["idx"].cpu().numpy(), vals, W["x"].cpu().numpy(),
+                          None if h_sc is None else h_sc.numpy())
+    bad = int(np.sum(np.abs(h_y.numpy().astype(np.float64) - y64) > fp32_bound(off, yabs)))
     if bad:
-        raise SystemExit(f"el_spmv_host output fails the oracle bound in {bad} rows")
+        raise SystemExit(f"el_spmv_host output fails the FP64 bound in {bad} rows")
     return {"value": round(world * nbytes / (ms * 1e-3) / 1e9, 2), "unit": "GB/s",
             "ms_per_step": round(ms, 4), "steps": steps,
             "h2d_bytes_per_step": int(world * h2d), "d2h_bytes_per_step": int(world * d2h),
@@ -550,7 +663,51 @@ def run_reference(args, rank, world):
                        f"in oracle/oracle.c, rows split over {threads} threads")},
         "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "reference_gpu_kernel": reference_gpu_kernel(W, nbytes, args),
     }
+
+
+def reference_gpu_kernel(W, nbytes, args):
+    """The reference's own merge_path_flat CUDA kernel on the same matrix
+    (the cubin oracle/ref/build_ref.sh compiles from the reference's
+    headers, launched as the reference's launcher launches it; y zeroed and
+    the L2 flushed before every run, outside the CUDA events), reported
+    beside the CPU loop.  None of this library's code runs here."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return {"unavailable": "no GPU"}
+        from oracle.ref import ref_gpu
+        if not ref_gpu.available():
+            return {"unavailable": "oracle/_ref/ref_kernels.cubin is not built here (it is "
+                                   "compiled from the reference's sources where they exist)"}
+        dev = torch.device("cuda", 0)
+        off, idx, vals, x = (ref_gpu.pad(W[k].to(dev)) for k in ("off", "idx", "vals", "x"))
+        rows, cols, nnz = W["rows"], W["cols"], int(W["idx"].numel())
+        y = ref_gpu.pad(torch.zeros(rows, device=dev))
+        R = ref_gpu.RefKernels()
+        flush = torch.empty(L2_FLUSH_BYTES // 4, device=dev)
+        stream = torch.cuda.current_stream()
+        steps = max(5, min(args.steps, 20))
+        ts = []
+        for k in range(steps + 3):
+            flush.fill_(float(k))
+            y.zero_()
+            s = torch.cuda.Event(enable_timing=True)
+            e = torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            R.launch("merge_path_flat", rows, cols, nnz, off, idx, vals, x, y, zero=False)
+            e.record(stream)
+            torch.cuda.synchronize()
+            if k >= 3:
+                ts.append(s.elapsed_time(e))
+        ms = statistics.median(ts)
+        return {"kernel": "loops::algorithms::spmv::__merge_path_flat<128, 5> (the reference's "
+                          "CUDA kernel, compiled from its headers for sm_103a)",
+                "us": round(ms * 1e3, 2), "GBps": round(nbytes / (ms * 1e-3) / 1e9, 2),
+                "steps": steps}
+    except Exception as e:  # the reference kernel is a side measurement
+        return {"unavailable": f"{type(e).__name__}: {e}"[:200]}
 
 
 # ------------------------------------------------------ SpMM and batched SpMV
@@ -578,7 +735,6 @@ def run_spmm(args):
     nonzeros (Zipf 2.0, cap 100000, seed 3), B dense row-major 2^20 x n."""
     import numpy as np
     import torch
-    import oracle
     from edge_loops_gb300 import api, synth
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
@@ -600,21 +756,24 @@ def run_spmm(args):
                       args.steps, args.warmup, flush, torch.cuda.current_stream())
     if ws.errors():
         raise SystemExit("device error flags in SpMM")
-    # parity on a sample of 2048 rows: FP64 oracle of those rows
+    # parity on a sample of 2048 rows: FP64 of those rows
     rng = np.random.default_rng(0)
     rows_s = np.sort(rng.choice(A.rows, 2048, replace=False))
     offh, idxh, valh = off.cpu().numpy(), idx.cpu().numpy(), vals.cpu().numpy()
     lens = offh[rows_s + 1] - offh[rows_s]
-    so = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
     sel = np.concatenate([np.arange(offh[r], offh[r + 1]) for r in rows_s])
+    row_of = np.repeat(np.arange(len(rows_s)), lens)
     Bh = B.float().cpu().numpy()
-    C64, Ca = oracle.spmm_f64(so, idxh[sel], valh[sel], Bh)
+    prod = valh[sel].astype(np.float64)[:, None] * Bh[idxh[sel]].astype(np.float64)
+    C64 = np.zeros((len(rows_s), args.n))
+    Ca = np.zeros((len(rows_s), args.n))
+    np.add.at(C64, row_of, prod)
+    np.add.at(Ca, row_of, np.abs(prod))
     got = Cm[torch.as_tensor(rows_s, device=dev)].cpu().numpy().astype(np.float64)
-    u = 2.0 ** -24
-    nn = (np.diff(so.astype(np.int64)) + 2)[:, None]
-    bad = int(np.sum(np.abs(got - C64) > (nn * u / (1 - nn * u)) * Ca))
+    so = np.concatenate([[0], np.cumsum(lens)])
+    bad = int(np.sum(np.abs(got - C64) > fp32_bound(so, 1.0)[:, None] * Ca))
     if bad:
-        raise SystemExit(f"SpMM output fails the oracle bound in {bad} entries")
+        raise SystemExit(f"SpMM output fails the FP64 bound in {bad} entries")
     peak, kind = measured_peaks()
     ach = compulsory / (ms * 1e-3) / 1e9
     return {
@@ -638,115 +797,134 @@ def run_spmm(args):
     }
 
 
-def run_batched(args):
-    """Batched SpMV (the batched workload): 4096 square CSRs, rows log-uniform in
-    [64, 65536], log-normal row lengths (mean 8, sigma 1), seed 4; one
-    persistent launch replayed from a CUDA graph.  Also times the plain FP32
-    merge-path kernel launched once per matrix (the comparison the target is
-    defined against) and the batched FP32 plan."""
+def measure_batched(dev, steps, warmup, flush, stream, dtypes=("bf16",), row_scale=True,
+                    per_matrix=True):
+    """The batched workload: 4096 square CSRs (rows log-uniform in [64,
+    65536], log-normal row lengths with mean 8 and sigma 1, seed 4), one
+    plan for FP32 values and one per 16-bit dtype in `dtypes` (values and
+    per-row scales of every matrix quantized in one array each), each a
+    CUDA-graph replay of one persistent launch per step; with per_matrix,
+    also the plain FP32 merge-path kernel launched once per matrix (eagerly
+    and captured in one CUDA graph), the comparison the batching target is
+    defined against.  Every row of every matrix is checked against FP64:
+    FP32 within the order-free bound, 16-bit within that bound of its stored
+    values, and the max relative error against FP64 of the FP32 matrices is
+    reported."""
     import numpy as np
     import torch
-    import oracle
     from edge_loops_gb300 import api, synth
-    dev = torch.device("cuda", 0)
-    torch.cuda.set_device(dev)
     R, offc, idxc, valc, xc, rs, ns = synth.batched(count=4096, seed=4, device=dev)
     items32, y32 = api.batched_items(R, offc, idxc, valc, xc, rs, ns)
-    stream = torch.cuda.current_stream()
-    flush = torch.empty(L2_FLUSH_BYTES // 4, device=dev)
+    goff, gidx = synth.batch_as_one_csr(R, offc, idxc, rs, ns)
+    o, i, v, xh = (t.cpu().numpy() for t in (goff, gidx, valc, xc))
+    y64, yabs = fp64_spmv(o, i, v, xh)
+    bound = fp32_bound(o, yabs)
 
     def total_bytes(items, vb, scaled):
         return sum(synth.algorithmic_bytes(A.rows, A.cols, A.nnz, vb, row_scale=scaled)
                    for A, _, _ in items)
 
+    thr = lambda b, t: round(b / (t * 1e-3) / 1e9, 2)  # noqa: E731
+    out = {"matrices": int(R.numel()), "rows_total": int(R.sum()), "nnz_total": int(idxc.numel())}
     b32 = total_bytes(items32, 4, False)
     plan32 = api.BatchPlan(items32)
-    ms32 = _time_device(plan32.execute, args.steps, args.warmup, flush, stream)
-    if args.value_dtype == "f32":
-        items, plan, ms, nb = items32, plan32, ms32, b32
-    else:
-        tdt = torch.bfloat16 if args.value_dtype == "bf16" else torch.float16
+    ms32 = _time_device(plan32.execute, steps, warmup, flush, stream)
+    if plan32.errors():
+        raise SystemExit("device error flags in the batched FP32 plan")
+    y = y32.cpu().numpy().astype(np.float64)
+    bad = int(np.sum(np.abs(y - y64) > bound))
+    comp, _ = rel_errors(y, y64, yabs)
+    if bad:
+        raise SystemExit(f"batched FP32 plan outside the FP32 bound in {bad} rows")
+    out["f32"] = {"ms": round(ms32, 4), "GBps": thr(b32, ms32), "algorithmic_bytes": b32,
+                  "plan": plan32.info(), "rows_outside_fp32_bound": bad,
+                  "max_rel_err_vs_fp64": comp}
+    for dt in dtypes:
+        tdt = torch.bfloat16 if dt == "bf16" else torch.float16
+        Q = api.CSR(goff, gidx, valc, goff.numel() - 1, goff.numel() - 1).quantized(
+            tdt, per_row_scale=row_scale)
         yq = torch.empty_like(y32)
-        # quantized values (and scales) of every matrix in one array each, at
-        # the element offsets of its indices (and rows)
-        vq = torch.empty(valc.numel(), dtype=tdt, device=dev)
-        sq = None if args.no_row_scale else torch.empty(y32.numel(), device=dev)
-        rs_l, ns_l = rs.tolist(), ns.tolist()
         items = []
-        for m, (A, x, _) in enumerate(items32):
-            r0, n0 = int(rs_l[m]), int(ns_l[m])
-            items.append((A.quantized(tdt, per_row_scale=sq is not None,
-                                      out=vq[n0: n0 + A.nnz],
-                                      out_scale=None if sq is None else sq[r0: r0 + A.rows]),
-                          x, yq[r0: r0 + A.rows]))
+        for m, (r, r0, n0) in enumerate(zip(R.tolist(), rs.tolist(), ns.tolist())):
+            nn = int(o[r0 + r] - o[r0])
+            items.append((api.CSR(offc[r0 + m: r0 + m + r + 1], idxc[n0: n0 + nn],
+                                  Q.values[n0: n0 + nn], r, r,
+                                  row_scale=None if Q.row_scale is None else
+                                  Q.row_scale[r0: r0 + r]),
+                          xc[r0: r0 + r], yq[r0: r0 + r]))
+        nb = total_bytes(items, 2, row_scale)
         plan = api.BatchPlan(items)
-        ms = _time_device(plan.execute, args.steps, args.warmup, flush, stream)
-        nb = total_bytes(items, 2, not args.no_row_scale)
-    if plan.errors() or plan32.errors():
-        raise SystemExit("device error flags in the batched plan")
-    # plain FP32 kernel, one launch per matrix
-    ws = api.Workspace()
+        ms = _time_device(plan.execute, steps, warmup, flush, stream)
+        if plan.errors():
+            raise SystemExit(f"device error flags in the batched {dt} plan")
+        yy = yq.cpu().numpy().astype(np.float64)
+        qv = Q.values.float().cpu().numpy()
+        sc = None if Q.row_scale is None else Q.row_scale.cpu().numpy()
+        yq64, yqabs = fp64_spmv(o, i, qv, xh, sc)
+        badq = int(np.sum(np.abs(yy - yq64) > fp32_bound(o, yqabs)))
+        compq, _ = rel_errors(yy, y64, yabs)
+        if badq or compq > 1e-2:
+            raise SystemExit(f"batched {dt} plan fails the check: {badq} rows, err {compq}")
+        out[dt] = {"ms": round(ms, 4), "GBps": thr(nb, ms), "algorithmic_bytes": nb,
+                   "plan": plan.info(), "rows_outside_fp32_bound_vs_stored": badq,
+                   "max_rel_err_vs_fp64_of_fp32_matrices": compq,
+                   "time_vs_fp32_plan": round(ms / ms32, 4)}
+        plan.close()
+        del plan, items, Q
+    plan32.close()
+    if per_matrix:
+        ws = api.Workspace()
 
-    def per_matrix():
-        for A, x, y in items32:
-            api.spmv(A, x, y, schedule="merge_path_flat", workspace=ws)
+        def one_by_one():
+            for A, x, yv in items32:
+                api.spmv(A, x, yv, schedule="merge_path_flat", workspace=ws)
 
-    per_steps = max(3, min(args.steps, 10))
-    per_matrix()  # sizes the workspace before capture
-    ms_plain_eager = _time_device(per_matrix, per_steps, 2, flush, stream)
-    # the same 4096 launches captured in one CUDA graph (no host overhead):
-    # the stricter comparison
-    graph = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(graph):
-        per_matrix()
-    ms_plain = _time_device(graph.replay, args.steps, args.warmup, flush, stream)
-    plan32.execute()
-    plan.execute()
-    torch.cuda.synchronize()
-    # parity: 512 sampled matrices against FP64 of the FP32 matrices
-    rng = np.random.default_rng(1)
-    worst, outside = 0.0, 0
-    for m in rng.choice(len(items), 512, replace=False):
-        A32, x, _ = items32[m]
-        A, _, y = items[m]
-        off = A32.offsets.cpu().numpy()
-        y64, yabs = oracle.spmv_f64(off, A32.indices.cpu().numpy(), A32.values.cpu().numpy(),
-                                    x.cpu().numpy())
-        yy = y.cpu().numpy().astype(np.float64)
-        worst = max(worst, oracle.error_metrics(yy, y64, yabs)[0])
-        if args.value_dtype == "f32":
-            u = 2.0 ** -24
-            n = np.diff(off.astype(np.int64)) + 2
-            outside += int(np.sum(np.abs(yy - y64) > (n * u / (1 - n * u)) * yabs))
-    if outside or worst > 1e-2:
-        raise SystemExit(f"batched output check failed: {outside} rows, max rel err {worst}")
+        one_by_one()  # sizes the workspace before capture
+        ms_eager = _time_device(one_by_one, max(3, min(steps, 10)), 2, flush, stream)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            one_by_one()
+        ms_graph = _time_device(graph.replay, steps, warmup, flush, stream)
+        if ws.errors():
+            raise SystemExit("device error flags in the per-matrix launches")
+        out["plain_f32_per_matrix"] = {
+            "graph_ms": round(ms_graph, 4), "graph_GBps": thr(b32, ms_graph),
+            "eager_ms": round(ms_eager, 4), "launches": len(items32)}
+        for dt in dtypes:
+            out[dt]["speedup_vs_plain_f32_per_matrix_graph"] = round(ms_graph / out[dt]["ms"], 3)
+            out[dt]["speedup_vs_plain_f32_per_matrix_eager"] = round(ms_eager / out[dt]["ms"], 3)
+        out["f32"]["speedup_vs_plain_f32_per_matrix_graph"] = round(ms_graph / ms32, 3)
+    return out
+
+
+def run_batched(args):
+    """Batched SpMV (the batched workload, measure_batched): the line's
+    value is the plan of --value-dtype."""
+    import torch
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, device=dev)
+    dts = () if args.value_dtype == "f32" else (args.value_dtype,)
+    r = measure_batched(dev, args.steps, args.warmup, flush, torch.cuda.current_stream(), dts,
+                        row_scale=not args.no_row_scale)
+    me = r[args.value_dtype]
     peak, kind = measured_peaks()
-    ach = nb / (ms * 1e-3) / 1e9
-    thr = lambda b, t: b / (t * 1e-3) / 1e9  # noqa: E731
     return {
         "metric": "batched SpMV achieved bandwidth (algorithmic bytes / graph time)",
-        "value": round(ach, 2), "unit": "GB/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True,
+        "value": me["GBps"], "unit": "GB/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": me["ms"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": f"{args.value_dtype} values, f32 accumulate",
         "data": "synthetic (seeded generator; SuiteSparse not available)",
         "config": {"workload": "4096 square CSRs, rows log-uniform [64, 65536], log-normal "
                                "nnz/row (mean 8, sigma 1), seed 4",
-                   "rows_total": int(R.sum()), "nnz_total": int(idxc.numel()),
-                   "algorithmic_bytes_per_step": nb, "plan": plan.info(),
+                   "rows_total": r["rows_total"], "nnz_total": r["nnz_total"],
+                   "algorithmic_bytes_per_step": me["algorithmic_bytes"], "plan": me["plan"],
                    "l2": "flushed before every step (512 MiB write, outside the timed graph)"},
-        "roofline": {"bound": "hbm", "achieved": round(ach, 2), "peak": peak, "unit": "GB/s",
-                     "frac": round(ach / peak, 4), "peak_source": kind,
+        "roofline": {"bound": "hbm", "achieved": me["GBps"], "peak": peak, "unit": "GB/s",
+                     "frac": round(me["GBps"] / peak, 4), "peak_source": kind,
                      "traffic": traffic_for(f"spmv_batched:{args.value_dtype}")},
-        "comparison": {
-            "batched_fp32_GBps": round(thr(b32, ms32), 2), "batched_fp32_ms": round(ms32, 4),
-            "plain_fp32_per_matrix_graph_GBps": round(thr(b32, ms_plain), 2),
-            "plain_fp32_per_matrix_graph_ms": round(ms_plain, 4),
-            "plain_fp32_per_matrix_eager_ms": round(ms_plain_eager, 4),
-            "speedup_vs_plain_fp32_per_matrix_graph": round(ms_plain / ms, 3),
-            "speedup_vs_plain_fp32_per_matrix_eager": round(ms_plain_eager / ms, 3),
-            "speedup_vs_batched_fp32": round(ms32 / ms, 3),
-            "max_rel_err_vs_fp64_of_fp32_matrices": worst},
+        "comparison": r,
         "gpu_launches": args.steps,
     }
 
@@ -755,11 +933,17 @@ def run_csr_build(args):
     """COO -> CSR on the GPU (el_csr_from_coo) for the power-law matrix's
     entries in random order: metric = COO bytes read + CSR bytes written per
     conversion time; checked entry by entry against the restated reference
-    construction (oracle.csr_from_coo)."""
+    construction (a stable sort by (row, column), offsets by lower bound;
+    container/csr.hxx:86-94) done with numpy."""
     import numpy as np
     import torch
-    import oracle
     from edge_loops_gb300 import api, synth
+
+    def csr_from_coo_np(rows, ri, ci, vv):
+        order = np.lexsort((ci, ri))  # stable
+        offs = np.searchsorted(ri[order], np.arange(rows + 1), side="left").astype(np.int32)
+        return offs, ci[order], vv[order]
+
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     off, idx, vals, x, cols = synth.power_law(rows=1 << 20, target_nnz=16_000_000, exponent=2.0,
@@ -778,15 +962,15 @@ def run_csr_build(args):
         out["A"] = api.csr_from_coo(rows, cols, ri, ci, vv, device=dev, workspace=ws)
     ms = _time_device(step, args.steps, args.warmup, flush, torch.cuda.current_stream())
     A = out["A"]
-    o2, i2, v2 = oracle.csr_from_coo(rows, ri.cpu().numpy(), ci.cpu().numpy(), vv.cpu().numpy())
+    o2, i2, v2 = csr_from_coo_np(rows, ri.cpu().numpy(), ci.cpu().numpy(), vv.cpu().numpy())
     ok = (np.array_equal(A.offsets.cpu().numpy(), o2) and np.array_equal(A.indices.cpu().numpy(), i2)
           and np.array_equal(A.values.cpu().numpy(), v2))
     if not ok:
-        raise SystemExit("el_csr_from_coo differs from the restated reference construction")
+        raise SystemExit("el_csr_from_coo differs from the numpy construction")
     nbytes = nnz * 12 + nnz * 8 + (rows + 1) * 4
     import time as _t
     t0 = _t.perf_counter()
-    oracle.csr_from_coo(rows, ri.cpu().numpy(), ci.cpu().numpy(), vv.cpu().numpy())
+    csr_from_coo_np(rows, ri.cpu().numpy(), ci.cpu().numpy(), vv.cpu().numpy())
     cpu_s = _t.perf_counter() - t0
     return {
         "metric": "COO->CSR construction bandwidth (COO read + CSR written / time)",
@@ -797,7 +981,7 @@ def run_csr_build(args):
         "config": {"workload": "COO of the 2^20 x 2^20 power-law matrix (seed 1), shuffled",
                    "nnz": nnz, "rows": rows, "bytes_per_step": nbytes,
                    "includes": "range check (one host sync), radix sort, gather, offsets"},
-        "check": {"equal_to_oracle": ok},
+        "check": {"equal_to_numpy_construction": ok},
         "cpu_baseline": {"value": round(nbytes / cpu_s / 1e9, 3), "unit": "GB/s", "cores": 1,
                          "kind": "port", "sample": "numpy stable lexsort + searchsorted, once"},
         "gpu_launches": 3 * args.steps,  # this library's kernels; the radix sort is CUB's
@@ -812,7 +996,6 @@ def run_edge(args):
     order-free bound; the partition build is timed once beside it."""
     import numpy as np
     import torch
-    import oracle
     from edge_loops_gb300 import api, edge, synth
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
@@ -839,17 +1022,17 @@ def run_edge(args):
                       args.warmup, flush, torch.cuda.current_stream())
     flags = api.workspace_errors(ws)
     o, i, v, xh = (t.cpu().numpy() for t in (off, idx, vals, x))
-    y64, yabs = oracle.spmv_f64(o, i, v, xh)
-    lens = np.diff(o).astype(np.float64)
-    bound = (lens + 8) * 2.0 ** -24 / (1 - (lens + 8) * 2.0 ** -24) * yabs
+    y64, yabs = fp64_spmv(o, i, v, xh)
+    bound = fp32_bound(o, yabs, extra=8)
     ok = flags == 0 and bool(np.all(np.abs(y.cpu().numpy().astype(np.float64) - y64) <= bound))
     if not ok:
-        raise SystemExit("el_spmv_edge outside the FP32 bound of the FP64 oracle")
-    comp, _ = oracle.error_metrics(y.cpu().numpy(), y64, yabs)
+        raise SystemExit("el_spmv_edge outside the FP32 bound of FP64")
+    comp, _ = rel_errors(y.cpu().numpy(), y64, yabs)
     rows, nnz = A.rows, A.nnz
     nbytes = nnz * 16 + 4 * cols + 4 * rows
     peak, src = measured_peaks()
     import time as _t
+    import oracle  # the CPU baseline: the reference's loop, restated
     t0 = _t.perf_counter()
     oracle.spmv_f32(o, i, v, xh)
     cpu_s = _t.perf_counter() - t0
@@ -894,6 +1077,8 @@ def main():
     ap.add_argument("--n", type=int, default=128, help="SpMM: columns of B")
     ap.add_argument("--b-dtype", default="f32", choices=["f32", "bf16", "f16"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-secondary", dest="secondary", action="store_false",
+                    help="default workload: skip the stencil and batched configurations")
     ap.add_argument("--e2e-block-nnz", type=int, default=0,
                     help="e2e: nonzeros per streamed row block (0: the library's default)")
     ap.add_argument("--edge", default="pos:256:1",
@@ -913,8 +1098,6 @@ def main():
     import torch
     from edge_loops_gb300 import build as b
     b.build()
-    import oracle
-    oracle.build()
     if world > 1:
         torch.distributed.init_process_group(
             "nccl", device_id=torch.device("cuda", _env_int("LOCAL_RANK", 0)))

@@ -162,6 +162,7 @@ SIGNATURES = {
     "el_batch_plan_destroy": (C.c_int, [C.c_void_p]),
     "el_spmv_static_scratch": (C.c_int, [C.POINTER(ElCsr), C.c_void_p, C.c_void_p, C.c_int32,
                                          C.POINTER(C.c_uint32), C.c_void_p]),
+    "el_spmv_static_scratch_errors": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.c_int]),
     "el_spmv_host": (C.c_int, [C.c_void_p, C.POINTER(ElCsr), C.c_int32, C.POINTER(ElSpmvOpts),
                                C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     "el_read_matrix_market": (C.c_int, [C.c_char_p, C.POINTER(ElCoo)]),

@@ -8,10 +8,8 @@
 // carry slots.  It is a module-scope __device__ array, so every GPU that
 // loads this library holds it (64 KiB + 64 B) until the process exits, and
 // every call on a device shares it.  Host code may not use the array's name
-// as a device address: the address is looked up once per device with
-// cudaGetSymbolAddress while that device is current.
-#include <mutex>
-
+// as a device address: every call looks the address up with
+// cudaGetSymbolAddress while the device is current.
 #include "el_internal.h"
 #include "spmv_merge_path_nz.cuh"
 
@@ -23,20 +21,16 @@ constexpr size_t kStaticBytes = sizeof(WsHeader) + (size_t)kStaticRanges * sizeo
 
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
 
-std::mutex g_static_mu;
-void* g_static_addr[256] = {nullptr};
-
-// Device address of g_static_scratch on `device` (which must be current).
-el_status static_scratch(int device, void** out) {
-  if (device < 0 || device >= 256) return fail(EL_ERR_INVALID_ARGUMENT, "device %d", device);
-  std::lock_guard<std::mutex> lk(g_static_mu);
-  if (!g_static_addr[device]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(static scratch)");
-    g_static_addr[device] = p;
-  }
-  *out = g_static_addr[device];
+// Device address of g_static_scratch on the current device.  Looked up on
+// every call rather than cached: after a cudaDeviceReset the library's
+// device image is loaded again (on the next call), possibly at another
+// address, and a cached pointer would be stale.  Only the first lookup on a
+// device (or the first after a reset) loads anything.
+el_status static_scratch(void** out) {
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(static scratch)");
+  *out = p;
   return EL_OK;
 }
 
@@ -105,7 +99,7 @@ extern "C" el_status el_spmv_static_scratch(const el_csr* A, const float* x, flo
   cudaError_t e = cudaGetDevice(&device);
   if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
   void* scratch = nullptr;
-  el_status s = static_scratch(device, &scratch);
+  el_status s = static_scratch(&scratch);
   if (s != EL_OK) return s;
   cudaStream_t st = (cudaStream_t)stream;
   // ticket, finished counter, error flags and their info start at zero each
@@ -126,4 +120,24 @@ extern "C" el_status el_spmv_static_scratch(const el_csr* A, const float* x, flo
   if (e != cudaSuccess) return cuda_status(e, "reading the static scratch flags");
   *flags = h;
   return h ? fail(EL_ERR_DEVICE, "device flags 0x%x", h) : EL_OK;
+}
+
+extern "C" el_status el_spmv_static_scratch_errors(el_stream_t stream, uint32_t* flags,
+                                                   int clear) {
+  if (!flags) return fail(EL_ERR_NULL_POINTER, "flags is NULL");
+  void* scratch = nullptr;
+  el_status s = static_scratch(&scratch);
+  if (s != EL_OK) return s;
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_status(e, "cudaStreamSynchronize");
+  unsigned h = 0;
+  char* errs = reinterpret_cast<char*>(scratch) + offsetof(WsHeader, errors);
+  e = cudaMemcpy(&h, errs, sizeof(h), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(e, "reading the static scratch flags");
+  *flags = h;
+  if (clear && h) {
+    e = cudaMemset(errs, 0, 2 * sizeof(unsigned));
+    if (e != cudaSuccess) return cuda_status(e, "clearing the static scratch flags");
+  }
+  return EL_OK;
 }

@@ -167,6 +167,28 @@ def batched(count=4096, rows_lo=64, rows_hi=65536, mean_per_row=8.0, sigma=1.0, 
     return rows, off_cat, idx, vals, x, row_start, nz_start
 
 
+def batch_as_one_csr(rows, off_cat, idx_cat, row_start, nz_start):
+    """A batch from batched() as one block-diagonal CSR over all its rows:
+    global offsets (matrix m's local offsets plus its first nonzero) and
+    global column indices (matrix m's columns plus its first row; the
+    matrices are square, so the batch's x and y are one vector each).
+    Returns (offsets int32[R + 1], indices int32[nnz]) on the batch's
+    device."""
+    count = rows.numel()
+    dev = off_cat.device
+    R = int(rows.sum())
+    nnz = idx_cat.numel()
+    mat_of_row = torch.repeat_interleave(torch.arange(count, device=dev), rows)
+    p = torch.arange(R, device=dev)
+    goff = torch.empty(R + 1, dtype=torch.int64, device=dev)
+    goff[:-1] = off_cat[p + mat_of_row].long() + nz_start[mat_of_row]
+    goff[-1] = nnz
+    nnz_m = torch.diff(torch.cat([nz_start, torch.tensor([nnz], device=dev)]))
+    mat_of_nz = torch.repeat_interleave(torch.arange(count, device=dev), nnz_m)
+    gidx = idx_cat.long() + row_start[mat_of_nz]
+    return goff.to(torch.int32), gidx.to(torch.int32)
+
+
 def algorithmic_bytes(rows, cols, nnz, value_bytes=4, row_scale=False):
     """Compulsory bytes of one SpMV: values + indices, offsets, x once, y
     written once (+ per-row scales)."""

@@ -487,23 +487,31 @@ el_status el_batch_plan_destroy(el_batch_plan* plan);
  * Its scratch (range tickets, error flags and one carry slot per warp
  * range) is a fixed array in the library's device image: 64 KiB + 64 B,
  * present on every GPU that loads the library until the process exits.
- * The first call on a device looks the array's device address up
- * (cudaGetSymbolAddress), so make that first call before any stream
- * capture.  All calls on a device share the array: calls that may overlap
- * on the GPU (other streams, other host threads) race and give wrong
- * results; serialise them.  Each call clears the array's counters and
- * flags itself.
+ * Each call looks the array's device address up (cudaGetSymbolAddress);
+ * the first call on a device, and the first after a cudaDeviceReset, also
+ * loads the library's device image there, so make that call before any
+ * stream capture.  All calls on a device share the array: calls that may
+ * overlap on the GPU (other streams, other host threads) race and give
+ * wrong results; serialise them.  Each call clears the array's counters
+ * and flags itself.
  *
  * num_ranges: warp ranges the work is split into, 0 = one per resident
  * warp (at most EL_STATIC_MAX_RANGES); a larger value is rejected with
  * EL_ERR_INVALID_ARGUMENT.  With flags != NULL the call synchronises
  * `stream`, stores the EL_FLAG_* bits the kernel raised and returns
- * EL_ERR_DEVICE if any is set; with flags == NULL it is asynchronous.
+ * EL_ERR_DEVICE if any is set; with flags == NULL it is asynchronous, and
+ * the bits stay readable with el_spmv_static_scratch_errors until the next
+ * call clears them.
  * Values FP32 / BF16 / FP16 with optional row scales; FP32 accumulation. */
 #define EL_STATIC_MAX_RANGES 4096
 el_status el_spmv_static_scratch(const el_csr* A, const float* x, float* y,
                                  int32_t num_ranges, uint32_t* flags,
                                  el_stream_t stream);
+/* Synchronises `stream` and returns the EL_FLAG_* bits the last
+ * el_spmv_static_scratch call on the current device raised (clearing them
+ * when clear != 0).  Allocates nothing. */
+el_status el_spmv_static_scratch_errors(el_stream_t stream, uint32_t* flags,
+                                        int clear);
 
 /* ---- mixed precision -------------------------------------------------- */
 /* Converts FP32 values to BF16 / FP16 (round to nearest even).  With

@@ -1,11 +1,12 @@
 #!/usr/bin/env bash
 # Builds oracle/_ref/ref_fixtures and oracle/_ref/ref_partition from the
 # reference's own headers (host code only; nvcc is used because the
-# reference's headers include the CUDA runtime and thrust). Needs the reference sources at $LOOPS_REF (default
-# /root/reference); outputs go only to oracle/_ref/ (git-ignored).
+# reference's headers include the CUDA runtime and thrust). Needs the reference sources at $LOOPS_REF
+# (default: a `reference` folder beside this repository's folder); outputs go only to oracle/_ref/
+# (git-ignored).
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
-ref="${LOOPS_REF:-/root/reference}"
+ref="${LOOPS_REF:-$here/../../../reference}"
 out="$here/../_ref"
 [ -d "$ref/include/loops" ] || { echo "reference sources not found at $ref" >&2; exit 3; }
 mkdir -p "$out"

@@ -58,7 +58,8 @@ def exact_spmv(offsets, indices, values, x):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=os.environ.get("LOOPS_REF", "/root/reference"))
+    from oracle.ref import sources
+    ap.add_argument("--ref", default=sources())
     args = ap.parse_args()
     env = dict(os.environ, LOOPS_REF=args.ref)
     subprocess.check_call([os.path.join(REPO, "oracle", "ref", "build_ref.sh")], env=env)

@@ -57,3 +57,24 @@ def test_cpu_baseline_line_on_a_small_matrix():
     assert line["unit"] == "GB/s" and line["kind"] == "port" and line["cores"] == 2
     assert line["value"] > 0 and line["single_thread"]["value"] > 0
     assert "helpers.hxx:106-112" in line["sample"]
+
+
+def test_fp64_checker_matches_the_oracle(oracle_mod):
+    """bench.py checks its outputs with its own FP64 evaluation; it must agree
+    with the oracle's FP64 loop (empty rows, row scales, row blocks that cut
+    the matrix into several chunks)."""
+    import numpy as np
+    from conftest import random_csr
+    b = _bench()
+    rng = np.random.default_rng(4)
+    off, idx, vals, x = random_csr(rng, rows=900, cols=700, max_len=40, empty_frac=0.25,
+                                   long_rows=[(3, 600)])
+    scale = np.exp2(rng.integers(-3, 4, size=900)).astype(np.float32)
+    for sc in (None, scale):
+        y, ya = b.fp64_spmv(off, idx, vals, x, sc, chunk=1000)
+        y0, ya0 = oracle_mod.spmv_f64(off, idx, vals, x, row_scale=sc)
+        np.testing.assert_allclose(y, y0, rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(ya, ya0, rtol=1e-12, atol=1e-12)
+    c, n = b.rel_errors(y0.astype(np.float32), y0, ya0)
+    c0, n0 = oracle_mod.error_metrics(y0.astype(np.float32), y0, ya0)
+    assert abs(c - c0) <= 1e-15 and abs(n - n0) <= 1e-15

@@ -10,10 +10,11 @@ import numpy as np
 import pytest
 
 from conftest import REPO, load_golden
+from oracle.ref import sources as ref_sources
 
 NVCC = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-REF = os.environ.get("LOOPS_REF", "/root/reference")
+REF = ref_sources()
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "include", "loops")),

@@ -108,26 +108,6 @@ def test_spmm_power_law_8M(cuda, oracle_mod, n, bdt):
         del Cm
 
 
-def _batch_as_one_csr(R, offc, idxc, rs, ns):
-    """The batch as one block-diagonal CSR over all its rows, on the device:
-    global offsets (matrix m's local offsets plus its first nonzero) and
-    global columns (matrix m's columns plus its first row; the matrices are
-    square, so x and y of the batch are one concatenated vector each)."""
-    count = R.numel()
-    dev = offc.device
-    rows_tot = int(R.sum())
-    nnz = idxc.numel()
-    mat_of_row = torch.repeat_interleave(torch.arange(count, device=dev), R)
-    p = torch.arange(rows_tot, device=dev)
-    goff = torch.empty(rows_tot + 1, dtype=torch.int64, device=dev)
-    goff[:-1] = offc[p + mat_of_row].long() + ns[mat_of_row]
-    goff[-1] = nnz
-    nnz_m = torch.diff(torch.cat([ns, torch.tensor([nnz], device=dev)]))
-    mat_of_nz = torch.repeat_interleave(torch.arange(count, device=dev), nnz_m)
-    gidx = idxc.long() + rs[mat_of_nz]
-    return goff.to(torch.int32), gidx.to(torch.int32)
-
-
 def test_batched_4096_matrices_f32_and_bf16(cuda, oracle_mod):
     """The batched workload at full size: 4096 square CSRs (rows log-uniform
     in [64, 65536], log-normal row lengths with mean 8, seed 4, ~310M
@@ -145,7 +125,7 @@ def test_batched_4096_matrices_f32_and_bf16(cuda, oracle_mod):
     plan.execute()
     torch.cuda.synchronize()
     assert plan.errors() == 0
-    goff, gidx = _batch_as_one_csr(R, offc, idxc, rs, ns)
+    goff, gidx = synth.batch_as_one_csr(R, offc, idxc, rs, ns)
     o, i, v, xh, yh = _host(goff, gidx, valc, xc, y)
     y64, yabs = oracle_mod.spmv_f64(o, i, v, xh)
     bad = np.nonzero(np.abs(yh.astype(np.float64) - y64) > order_free_bound(o, yabs))[0]

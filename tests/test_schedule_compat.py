@@ -13,10 +13,11 @@ import subprocess
 import pytest
 
 from conftest import REPO
+from oracle.ref import sources as ref_sources
 
 NVCC = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-REF = os.environ.get("LOOPS_REF", "/root/reference")
+REF = ref_sources()
 DRIVER = os.path.join(REPO, "tests", "cpp", "schedule_compat_driver.cu")
 
 

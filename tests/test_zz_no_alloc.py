@@ -71,3 +71,28 @@ def test_static_scratch_range_limit_and_small_counts(cuda, oracle_mod):
         got = y.cpu().numpy().astype(np.float64)
         assert np.all(np.abs(got - y64) <= bound), ranges
         assert np.all(np.abs(got - ref) <= 2 * bound), ranges
+
+
+def test_static_scratch_errors_readable_after_async_call(cuda):
+    """With flags == NULL the call is asynchronous; el_spmv_static_scratch_errors
+    reads the bits it raised afterwards (here: a column index past the end,
+    which the kernel skips and reports), and the next call starts clean."""
+    from edge_loops_gb300 import _lib, api
+    L = _lib.lib()
+    off = np.array([0, 2, 3, 5], dtype=np.int32)
+    idx = np.array([0, 9, 1, 0, 2], dtype=np.int32)  # 9 >= cols
+    vals = np.ones(5, dtype=np.float32)
+    A = api.CSR.from_arrays(off, idx, vals, 3, device=cuda)
+    x = torch.ones(3, device=cuda)
+    y = torch.empty(3, device=cuda)
+    st, _ = _static_spmv(A, x, y, flags=False)
+    assert st == 0
+    f = C.c_uint32(0)
+    s = torch.cuda.current_stream().cuda_stream
+    assert L.el_spmv_static_scratch_errors(C.c_void_p(s), C.byref(f), 1) == 0
+    assert f.value & _lib.EL_FLAG_INDEX_RANGE
+    good = api.CSR.from_arrays(off, np.array([0, 2, 1, 0, 2], np.int32), vals, 3, device=cuda)
+    st, flags = _static_spmv(good, x, y)
+    assert st == 0 and flags == 0
+    np.testing.assert_array_equal(y.cpu().numpy(), [2, 1, 2])
+    assert L.el_spmv_static_scratch_errors(C.c_void_p(s), C.byref(f), 0) == 0 and f.value == 0
