@@ -18,6 +18,11 @@ nvcc -std=c++17 -O1 --expt-extended-lambda --expt-relaxed-constexpr -w \
 nvcc "$out/ref_fixtures.o" "$out/mmio.o" -o "$out/ref_fixtures"
 nvcc -std=c++17 -O1 --expt-extended-lambda --expt-relaxed-constexpr -w \
   -I"$ref/include" "$here/ref_partition.cu" -o "$out/ref_partition"
+# the reference's CPU SpMV (cpu::reference) with thrust's device system on
+# the host, so that it runs without a GPU; cxxopts replaced by a stand-in
+nvcc -std=c++17 -O3 --expt-extended-lambda --expt-relaxed-constexpr -w \
+  -DTHRUST_DEVICE_SYSTEM=THRUST_DEVICE_SYSTEM_CPP -I"$here/stub" -I"$ref/include" \
+  -I"$ref/examples/spmv" "$here/ref_cpu.cu" -o "$out/ref_cpu"
 # the reference's SpMV kernels as a cubin, the names of its entry functions
 # (as ptxas prints them) and the launch-parameter layout the host compiler
 # sees (a host program run here, no GPU needed)
@@ -44,4 +49,4 @@ layout = json.loads(subprocess.check_output([os.path.join(out, "ref_kernels_layo
 layout["kernels"] = kernels
 json.dump(layout, open(os.path.join(out, "ref_kernels.json"), "w"), indent=1)
 PY
-echo "built $out/ref_fixtures $out/ref_partition $out/ref_kernels.cubin"
+echo "built $out/ref_fixtures $out/ref_partition $out/ref_cpu $out/ref_kernels.cubin"
