@@ -798,7 +798,7 @@ def run_spmm(args):
 
 
 def measure_batched(dev, steps, warmup, flush, stream, dtypes=("bf16",), row_scale=True,
-                    per_matrix=True):
+                    per_matrix=True, count=4096):
     """The batched workload: 4096 square CSRs (rows log-uniform in [64,
     65536], log-normal row lengths with mean 8 and sigma 1, seed 4), one
     plan for FP32 values and one per 16-bit dtype in `dtypes` (values and
@@ -813,7 +813,7 @@ def measure_batched(dev, steps, warmup, flush, stream, dtypes=("bf16",), row_sca
     import numpy as np
     import torch
     from edge_loops_gb300 import api, synth
-    R, offc, idxc, valc, xc, rs, ns = synth.batched(count=4096, seed=4, device=dev)
+    R, offc, idxc, valc, xc, rs, ns = synth.batched(count=count, seed=4, device=dev)
     items32, y32 = api.batched_items(R, offc, idxc, valc, xc, rs, ns)
     goff, gidx = synth.batch_as_one_csr(R, offc, idxc, rs, ns)
     o, i, v, xh = (t.cpu().numpy() for t in (goff, gidx, valc, xc))
@@ -906,7 +906,8 @@ def run_batched(args):
     flush = torch.empty(L2_FLUSH_BYTES // 4, device=dev)
     dts = () if args.value_dtype == "f32" else (args.value_dtype,)
     r = measure_batched(dev, args.steps, args.warmup, flush, torch.cuda.current_stream(), dts,
-                        row_scale=not args.no_row_scale)
+                        row_scale=not args.no_row_scale, per_matrix=args.batch_count == 4096,
+                        count=args.batch_count)
     me = r[args.value_dtype]
     peak, kind = measured_peaks()
     return {
@@ -916,14 +917,15 @@ def run_batched(args):
         "scaling": "weak", "vs_baseline": None,
         "dtype": f"{args.value_dtype} values, f32 accumulate",
         "data": "synthetic (seeded generator; SuiteSparse not available)",
-        "config": {"workload": "4096 square CSRs, rows log-uniform [64, 65536], log-normal "
-                               "nnz/row (mean 8, sigma 1), seed 4",
+        "config": {"workload": f"{args.batch_count} square CSRs, rows log-uniform [64, 65536], "
+                               "log-normal nnz/row (mean 8, sigma 1), seed 4",
                    "rows_total": r["rows_total"], "nnz_total": r["nnz_total"],
                    "algorithmic_bytes_per_step": me["algorithmic_bytes"], "plan": me["plan"],
                    "l2": "flushed before every step (512 MiB write, outside the timed graph)"},
         "roofline": {"bound": "hbm", "achieved": me["GBps"], "peak": peak, "unit": "GB/s",
                      "frac": round(me["GBps"] / peak, 4), "peak_source": kind,
-                     "traffic": traffic_for(f"spmv_batched:{args.value_dtype}")},
+                     "traffic": traffic_for(f"spmv_batched:{args.value_dtype}" + (
+                         "" if args.batch_count == 4096 else f":{args.batch_count}"))},
         "comparison": r,
         "gpu_launches": args.steps,
     }
@@ -1075,6 +1077,9 @@ def main():
     ap.add_argument("--no-row-scale", action="store_true",
                     help="16-bit values without per-row scales")
     ap.add_argument("--n", type=int, default=128, help="SpMM: columns of B")
+    ap.add_argument("--batch-count", type=int, default=4096,
+                    help="spmv_batched: matrices in the batch (the workload has 4096; fewer "
+                         "for profiler captures)")
     ap.add_argument("--b-dtype", default="f32", choices=["f32", "bf16", "f16"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-secondary", dest="secondary", action="store_false",

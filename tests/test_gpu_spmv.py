@@ -26,6 +26,7 @@ SCHEDS = [
     ("work_oriented", {}),
     ("work_oriented", {"num_threads": 1024}),
     ("thread_mapped", {}),
+    ("thread_mapped", {"compensated": True}),
     ("thread_mapped", {"threads_per_row": 8}),
     ("thread_mapped", {"threads_per_row": 32}),
     ("group_mapped", {}),
@@ -83,11 +84,34 @@ def test_uniform_1000_matches_reference_cpu(cuda, oracle_mod, sched, opts):
     check_against_oracle(oracle_mod, off, idx, vals, x, y)
 
 
-def test_thread_mapped_bit_exact_with_reference_loop(cuda, oracle_mod):
+def _tm_cases():
+    from edge_loops_gb300 import synth
     rng = np.random.default_rng(21)
-    off, idx, vals, x = random_csr(rng, rows=5000, cols=3000, max_len=60, empty_frac=0.1)
-    A = dev_csr(off, idx, vals, 3000, cuda)
-    y, _ = run(A, x, "thread_mapped", {}, cuda)
+    yield "random", random_csr(rng, rows=5000, cols=3000, max_len=60, empty_frac=0.1), 3000
+    o, i, v, x, n = synth.stencil27(n=24, seed=2)
+    yield "stencil24", (o.numpy(), i.numpy(), v.numpy(), x.numpy()), n
+    o, i, v, x, cols = synth.power_law(rows=1 << 14, target_nnz=300_000, cap=20_000, seed=5)
+    yield "power_law", (o.numpy(), i.numpy(), v.numpy(), x.numpy()), cols
+    # rows of every length from 0 to 70 around the 8-nonzero load batches
+    lens = np.concatenate([np.arange(71), rng.integers(0, 70, 100)])
+    off = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    idx = np.concatenate([np.sort(rng.choice(500, L, replace=False)) for L in lens]).astype(np.int32)
+    yield "row_lengths", (off, idx, rng.uniform(-1, 1, len(idx)).astype(np.float32),
+                          rng.uniform(-1, 1, 500).astype(np.float32)), 500
+
+
+@pytest.mark.parametrize("case", ["random", "stencil24", "power_law", "row_lengths"])
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+def test_thread_mapped_bit_exact_with_reference_loop(cuda, oracle_mod, case, dtype):
+    """One lane per row: y is the reference CPU loop's, bit for bit (16-bit
+    values: the loop over their exact FP32 widening)."""
+    (off, idx, vals, x), cols = next(c[1:] for c in _tm_cases() if c[0] == case)
+    A = dev_csr(off, idx, vals, cols, cuda)
+    if dtype != torch.float32:
+        A = A.quantized(dtype, per_row_scale=False)
+        vals = A.values.float().cpu().numpy()
+    y, flags = run(A, x, "thread_mapped", {}, cuda)
+    assert flags == 0
     np.testing.assert_array_equal(y, oracle_mod.spmv_f32(off, idx, vals, x))
 
 
