@@ -388,7 +388,8 @@ def run_secondary(args, dev):
         gbps = nb / (ms * 1e-3) / 1e9
         st[dt] = {"us": round(ms * 1e3, 2), "GBps": round(gbps, 1), "frac": round(gbps / peak, 4),
                   "algorithmic_bytes": nb, "rows_outside_fp32_bound": bad,
-                  "max_rel_err_vs_fp64_of_fp32_matrix": comp}
+                  "max_rel_err_vs_fp64_of_fp32_matrix": comp,
+                  "traffic": traffic_for(f"spmv_stencil:merge_path_flat:{dt}")}
         del Q, y
     for dt in ("bf16", "f16"):
         st[dt]["time_vs_f32"] = round(st[dt]["us"] / st["f32"]["us"], 4)
@@ -401,6 +402,7 @@ def run_secondary(args, dev):
                      "(mean 8, sigma 1), seed 4; one persistent launch per plan in a CUDA graph")
     for dt in ("f32", "bf16"):
         b[dt]["frac"] = round(b[dt]["GBps"] / peak, 4)
+        b[dt]["traffic"] = traffic_for(f"spmv_batched:{dt}")
     out["batched4096"] = b
     torch.cuda.empty_cache()
     return out

@@ -126,6 +126,7 @@ def tune(dtype="bf16", target_nnz=16_000_000, seed=100, verbose=True):
                 if not res:
                     continue
                 ms, tpr, cl = min(res)
+                fastest = (tpr, cl, ms)
                 # the built-in rule unless a choice beats it clearly: a bucket's
                 # optimum measured alone moves by a few per cent inside a mixed
                 # batch, so small gains are noise
@@ -136,7 +137,7 @@ def tune(dtype="bf16", target_nnz=16_000_000, seed=100, verbose=True):
                 # two groups landing in one bucket: keep the choice of the
                 # group nearer the bucket's centre (the first one probed)
                 if prev is None:
-                    best[key] = (tpr, cl, ms)
+                    best[key] = (tpr, cl, ms, fastest, base[0] if base else None)
                 if verbose:
                     print(f"rows {r:6d} mean {mean:7.1f} sigma {sg:.1f} -> bucket {key}: "
                           f"tpr {tpr} chunk 2^{cl} {ms:.4f} ms (built-in "
@@ -146,20 +147,25 @@ def tune(dtype="bf16", target_nnz=16_000_000, seed=100, verbose=True):
     # fill unprobed row buckets from the nearest probed one
     entries = {}
     probed_rb = sorted({k[0] for k in best})
-    for (rb, lb, cb), (tpr, cl, _) in best.items():
+    for (rb, lb, cb), (tpr, cl, *_rest) in best.items():
         if (tpr, cl) != BUILTIN:
             entries[f"{rb},{lb},{cb}"] = [tpr, cl]
     for rb in range(L.EL_BATCH_ROW_BUCKETS):
         if rb in probed_rb:
             continue
         near = min(probed_rb, key=lambda p: (abs(p - rb), p))
-        for (prb, lb, cb), (tpr, cl, _) in best.items():
+        for (prb, lb, cb), (tpr, cl, *_rest) in best.items():
             if prb == near and (tpr, cl) != BUILTIN:
                 entries.setdefault(f"{rb},{lb},{cb}", [tpr, cl])
+    # per probed bucket: the choice kept, the fastest (threads per row, chunk,
+    # ms) and the built-in rule's ms on the same group of matrices
     return {"dtype": dtype, "device": torch.cuda.get_device_name(dev),
             "threads_per_row": list(TPRS), "chunk_log2": list(CHUNKS),
-            "probed": {f"{k[0]},{k[1]},{k[2]}": [v[0], v[1], round(v[2], 5)]
-                       for k, v in sorted(best.items())},
+            "probed": {f"{k[0]},{k[1]},{k[2]}": {
+                "chosen": [v[0], v[1]],
+                "fastest": [v[3][0], v[3][1], round(v[3][2], 5)],
+                "builtin_ms": None if v[4] is None else round(v[4], 5)}
+                for k, v in sorted(best.items())},
             "entries": dict(sorted(entries.items(), key=lambda kv: tuple(
                 int(t) for t in kv[0].split(","))))}
 
