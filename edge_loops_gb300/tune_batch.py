@@ -7,11 +7,15 @@ loaded by api.load_tuning_table).
     python -m edge_loops_gb300.tune_batch [--dtype bf16] [--out PATH]
 
 Each probed bucket gets a group of synthetic matrices (fixed rows, log-normal
-row lengths with the bucket's mean and spread, ~16M nonzeros in total, so
-that one group fills the GPU as a whole batch does);
-every (kernel mode, log2 rows + nonzeros per work item) pair is timed as a
-CUDA-graph replay with L2 flushed before each replay, and a bucket gets an
-entry only where a choice beats the plan's built-in rule by MARGIN.  The
+row lengths with the bucket's mean and spread, ~16M nonzeros in total) and a
+second group twice as large; every (kernel mode, log2 rows + nonzeros per
+work item) pair is timed on both as a CUDA-graph replay with L2 flushed
+before each replay, and the choice is made on the difference: the marginal
+cost of the bucket's matrices.  (A group timed alone ends with a tail of
+about one work item per warp, which rewards small items; inside a whole
+batch each warp runs dozens of items and the tail is shared, so the
+marginal cost is what a bucket adds to a batch.)  A bucket gets an entry
+only where a choice beats the plan's built-in rule by MARGIN.  The
 bucket a group lands in is computed from its actual row statistics with the
 same rule the plan uses; row buckets that were not probed take the entry of
 the nearest probed row bucket with the same length and variation buckets.
@@ -105,7 +109,7 @@ def tune(dtype="bf16", target_nnz=16_000_000, seed=100, verbose=True):
             for sg in SIGMAS:
                 count = int(min(8192, max(16, target_nnz // max(1, int(r * mean)))))
                 rows, off, idx, vals, x, rs, ns = synth.batched(
-                    count=count, rows_lo=r, rows_hi=r, mean_per_row=mean, sigma=sg,
+                    count=2 * count, rows_lo=r, rows_hi=r, mean_per_row=mean, sigma=sg,
                     seed=seed, device=dev)
                 seed += 1
                 key = group_key(off, rows, rs)
@@ -116,13 +120,17 @@ def tune(dtype="bf16", target_nnz=16_000_000, seed=100, verbose=True):
                 res = []
                 for tpr in TPRS:
                     for cl in CHUNKS:
-                        plan = api.BatchPlan(items, table=None, force_threads_per_row=tpr,
-                                             force_chunk_log2=cl)
-                        if plan.info()["heavy_matrices"] == len(items):
+                        t = []
+                        for part in (items[:count], items):
+                            plan = api.BatchPlan(part, table=None, force_threads_per_row=tpr,
+                                                 force_chunk_log2=cl)
+                            if plan.info()["heavy_matrices"] == len(part):
+                                plan.close()
+                                break
+                            t.append(time_plan(plan, flush))
                             plan.close()
-                            continue
-                        res.append((time_plan(plan, flush), tpr, cl))
-                        plan.close()
+                        if len(t) == 2:
+                            res.append((t[1] - t[0], tpr, cl))
                 if not res:
                     continue
                 ms, tpr, cl = min(res)
@@ -140,9 +148,9 @@ def tune(dtype="bf16", target_nnz=16_000_000, seed=100, verbose=True):
                     best[key] = (tpr, cl, ms, fastest, base[0] if base else None)
                 if verbose:
                     print(f"rows {r:6d} mean {mean:7.1f} sigma {sg:.1f} -> bucket {key}: "
-                          f"tpr {tpr} chunk 2^{cl} {ms:.4f} ms (built-in "
-                          f"{base[0] if base else float('nan'):.4f}) ({time.time() - t0:.0f} s)",
-                          flush=True)
+                          f"tpr {tpr} chunk 2^{cl} marginal {ms:.4f} ms for {count} matrices "
+                          f"(built-in {base[0] if base else float('nan'):.4f}) "
+                          f"({time.time() - t0:.0f} s)", flush=True)
                 del items, y
     # fill unprobed row buckets from the nearest probed one
     entries = {}
@@ -158,7 +166,7 @@ def tune(dtype="bf16", target_nnz=16_000_000, seed=100, verbose=True):
             if prb == near and (tpr, cl) != BUILTIN:
                 entries.setdefault(f"{rb},{lb},{cb}", [tpr, cl])
     # per probed bucket: the choice kept, the fastest (threads per row, chunk,
-    # ms) and the built-in rule's ms on the same group of matrices
+    # marginal ms) and the built-in rule's marginal ms on the same matrices
     return {"dtype": dtype, "device": torch.cuda.get_device_name(dev),
             "threads_per_row": list(TPRS), "chunk_log2": list(CHUNKS),
             "probed": {f"{k[0]},{k[1]},{k[2]}": {
