@@ -400,6 +400,20 @@ def load_tuning_table(path=None):
     return t
 
 
+def batch_item_array(items, count=None):
+    """The el_batch_item array of a list of (CSR, x, y), for the first `count`
+    of them (all by default); the tensors must outlive every plan made from
+    it."""
+    n = len(items) if count is None else count
+    arr = (L.ElBatchItem * max(n, 1))()
+    for i in range(n):
+        A, x, y = items[i]
+        arr[i].A = A.el()
+        arr[i].x = x.data_ptr() if x is not None and x.numel() else None
+        arr[i].y = y.data_ptr() if y is not None and y.numel() else None
+    return arr
+
+
 class BatchPlan:
     """el_batch_plan: y_i = A_i x_i for many independent matrices in one
     persistent launch captured in a CUDA graph.  `items` is a list of
@@ -409,11 +423,7 @@ class BatchPlan:
                  force_chunk_log2=0, max_ctas=0, stream=None):
         import numpy as np
         self._keep = list(items)
-        arr = (L.ElBatchItem * max(len(items), 1))()
-        for i, (A, x, y) in enumerate(items):
-            arr[i].A = A.el()
-            arr[i].x = x.data_ptr() if x is not None and x.numel() else None
-            arr[i].y = y.data_ptr() if y is not None and y.numel() else None
+        arr = batch_item_array(items)
         o = L.ElBatchOpts()
         L.lib().el_batch_opts_default(C.byref(o))
         if isinstance(table, str) and table == "default":
@@ -425,9 +435,28 @@ class BatchPlan:
         o.force_chunk_log2 = force_chunk_log2
         o.max_ctas = max_ctas
         h = C.c_void_p()
-        L.check(L.lib().el_batch_plan_create(arr, len(items), C.byref(o), _stream(stream),
+        L.check(L.lib().el_batch_plan_create(arr, len(self._keep), C.byref(o), _stream(stream),
                                              C.byref(h)), "el_batch_plan_create")
         self.handle = h
+
+    @classmethod
+    def from_array(cls, arr, count, keep, force_threads_per_row=0, force_chunk_log2=0,
+                   use_graph=True, stream=None):
+        """A plan over the first `count` entries of a prebuilt
+        batch_item_array (no tuning table; `keep` holds the tensors)."""
+        self = cls.__new__(cls)
+        self._keep = keep
+        self._table = None
+        o = L.ElBatchOpts()
+        L.lib().el_batch_opts_default(C.byref(o))
+        o.use_graph = int(bool(use_graph))
+        o.force_threads_per_row = force_threads_per_row
+        o.force_chunk_log2 = force_chunk_log2
+        h = C.c_void_p()
+        L.check(L.lib().el_batch_plan_create(arr, count, C.byref(o), _stream(stream),
+                                             C.byref(h)), "el_batch_plan_create")
+        self.handle = h
+        return self
 
     def execute(self, stream=None):
         L.check(L.lib().el_batch_plan_execute(self.handle, _stream(stream)),
