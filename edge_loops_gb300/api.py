@@ -381,23 +381,28 @@ def work_oriented_partition(offsets, rows, nnz, num_threads, stream=None):
 
 
 # ---------------------------------------------------------------- batched SpMV
+def tuning_table(entries):
+    """int32[EL_BATCH_TABLE_SIZE] from {"rb,lb,cb": [threads_per_row, chunk_log2]}."""
+    import numpy as np
+    t = np.zeros(L.EL_BATCH_TABLE_SIZE, dtype=np.int32)
+    for key, (tpr, chunk_log2) in entries.items():
+        rb, lb, cb = (int(v) for v in key.split(","))
+        idx = (rb * L.EL_BATCH_LEN_BUCKETS + lb) * L.EL_BATCH_CV_BUCKETS + cb
+        t[idx] = int(tpr) | (int(chunk_log2) << 8)
+    return t
+
+
 def load_tuning_table(path=None):
     """The batched tuning table (int32[EL_BATCH_TABLE_SIZE]) from the JSON the
     tuner wrote (edge_loops_gb300/batch_tuning.json by default), or None."""
     import json
     import os
-    import numpy as np
     path = path or os.path.join(os.path.dirname(os.path.abspath(__file__)), "batch_tuning.json")
     if not os.path.exists(path):
         return None
     with open(path) as f:
         d = json.load(f)
-    t = np.zeros(L.EL_BATCH_TABLE_SIZE, dtype=np.int32)
-    for key, (tpr, chunk_log2) in d["entries"].items():
-        rb, lb, cb = (int(v) for v in key.split(","))
-        idx = (rb * L.EL_BATCH_LEN_BUCKETS + lb) * L.EL_BATCH_CV_BUCKETS + cb
-        t[idx] = int(tpr) | (int(chunk_log2) << 8)
-    return t
+    return tuning_table(d["entries"])
 
 
 def batch_item_array(items, count=None):
@@ -441,14 +446,17 @@ class BatchPlan:
 
     @classmethod
     def from_array(cls, arr, count, keep, force_threads_per_row=0, force_chunk_log2=0,
-                   use_graph=True, stream=None):
+                   use_graph=True, stream=None, table=None):
         """A plan over the first `count` entries of a prebuilt
-        batch_item_array (no tuning table; `keep` holds the tensors)."""
+        batch_item_array (`keep` holds the tensors; `table` an int32 tuning
+        table or None for the built-in rule)."""
+        import numpy as np
         self = cls.__new__(cls)
         self._keep = keep
-        self._table = None
+        self._table = None if table is None else np.ascontiguousarray(table, dtype=np.int32)
         o = L.ElBatchOpts()
         L.lib().el_batch_opts_default(C.byref(o))
+        o.table = self._table.ctypes.data if self._table is not None else None
         o.use_graph = int(bool(use_graph))
         o.force_threads_per_row = force_threads_per_row
         o.force_chunk_log2 = force_chunk_log2

@@ -7,18 +7,24 @@ loaded by api.load_tuning_table).
     python -m edge_loops_gb300.tune_batch [--dtype bf16] [--out PATH]
 
 Each probed bucket gets a group of synthetic matrices (fixed rows, log-normal
-row lengths with the bucket's mean and spread, ~16M nonzeros in total) and a
-second group twice as large; every (kernel mode, log2 rows + nonzeros per
-work item) pair is timed on both as a CUDA-graph replay with L2 flushed
-before each replay, and the choice is made on the difference: the marginal
-cost of the bucket's matrices.  (A group timed alone ends with a tail of
-about one work item per warp, which rewards small items; inside a whole
-batch each warp runs dozens of items and the tail is shared, so the
-marginal cost is what a bucket adds to a batch.)  A bucket gets an entry
-only where a choice beats the plan's built-in rule by MARGIN.  The
-bucket a group lands in is computed from its actual row statistics with the
-same rule the plan uses; row buckets that were not probed take the entry of
-the nearest probed row bucket with the same length and variation buckets.
+row lengths with the bucket's mean and spread, ~16M nonzeros in total);
+every (kernel mode, log2 rows + nonzeros per work item) pair is timed as a
+CUDA-graph replay with L2 flushed before each replay, and a bucket gets a
+candidate entry where a choice beats the plan's built-in rule by MARGIN.
+The bucket a group lands in is computed from its actual row statistics with
+the same rule the plan uses; row buckets that were not probed take the
+entry of the nearest probed row bucket with the same length and variation
+buckets.
+
+A group timed alone is not a batch: it ends with a tail of about one work
+item per warp, which rewards small items, while inside a batch of
+thousands of matrices each warp runs dozens of items.  So the candidates
+are validated on a mixed batch (the 4096-matrix generator of the batched
+benchmark with another seed): starting from the built-in rule, the
+candidates of one row bucket at a time are added to the table and kept
+only if the whole batch runs at least 1 % faster with them.  The table
+written holds the kept entries (possibly none: then the plan runs the
+built-in rule everywhere).
 """
 import argparse
 import json
@@ -109,7 +115,7 @@ def tune(dtype="bf16", target_nnz=16_000_000, seed=100, verbose=True):
             for sg in SIGMAS:
                 count = int(min(8192, max(16, target_nnz // max(1, int(r * mean)))))
                 rows, off, idx, vals, x, rs, ns = synth.batched(
-                    count=2 * count, rows_lo=r, rows_hi=r, mean_per_row=mean, sigma=sg,
+                    count=count, rows_lo=r, rows_hi=r, mean_per_row=mean, sigma=sg,
                     seed=seed, device=dev)
                 seed += 1
                 key = group_key(off, rows, rs)
@@ -117,20 +123,18 @@ def tune(dtype="bf16", target_nnz=16_000_000, seed=100, verbose=True):
                 if tdt != torch.float32:
                     items = [(A.quantized(tdt, per_row_scale=True), xx, yy)
                              for A, xx, yy in items]
+                arr = api.batch_item_array(items)
                 res = []
                 for tpr in TPRS:
                     for cl in CHUNKS:
-                        t = []
-                        for part in (items[:count], items):
-                            plan = api.BatchPlan(part, table=None, force_threads_per_row=tpr,
-                                                 force_chunk_log2=cl)
-                            if plan.info()["heavy_matrices"] == len(part):
-                                plan.close()
-                                break
-                            t.append(time_plan(plan, flush))
+                        plan = api.BatchPlan.from_array(arr, len(items), items,
+                                                        force_threads_per_row=tpr,
+                                                        force_chunk_log2=cl)
+                        if plan.info()["heavy_matrices"] == len(items):
                             plan.close()
-                        if len(t) == 2:
-                            res.append((t[1] - t[0], tpr, cl))
+                            continue
+                        res.append((time_plan(plan, flush), tpr, cl))
+                        plan.close()
                 if not res:
                     continue
                 ms, tpr, cl = min(res)
@@ -148,9 +152,9 @@ def tune(dtype="bf16", target_nnz=16_000_000, seed=100, verbose=True):
                     best[key] = (tpr, cl, ms, fastest, base[0] if base else None)
                 if verbose:
                     print(f"rows {r:6d} mean {mean:7.1f} sigma {sg:.1f} -> bucket {key}: "
-                          f"tpr {tpr} chunk 2^{cl} marginal {ms:.4f} ms for {count} matrices "
-                          f"(built-in {base[0] if base else float('nan'):.4f}) "
-                          f"({time.time() - t0:.0f} s)", flush=True)
+                          f"tpr {tpr} chunk 2^{cl} {ms:.4f} ms (built-in "
+                          f"{base[0] if base else float('nan'):.4f}) ({time.time() - t0:.0f} s)",
+                          flush=True)
                 del items, y
     # fill unprobed row buckets from the nearest probed one
     entries = {}
@@ -165,8 +169,8 @@ def tune(dtype="bf16", target_nnz=16_000_000, seed=100, verbose=True):
         for (prb, lb, cb), (tpr, cl, *_rest) in best.items():
             if prb == near and (tpr, cl) != BUILTIN:
                 entries.setdefault(f"{rb},{lb},{cb}", [tpr, cl])
-    # per probed bucket: the choice kept, the fastest (threads per row, chunk,
-    # marginal ms) and the built-in rule's marginal ms on the same matrices
+    # per probed bucket: the candidate, the fastest (threads per row, chunk,
+    # ms) and the built-in rule's ms on the same group of matrices
     return {"dtype": dtype, "device": torch.cuda.get_device_name(dev),
             "threads_per_row": list(TPRS), "chunk_log2": list(CHUNKS),
             "probed": {f"{k[0]},{k[1]},{k[2]}": {
@@ -176,6 +180,64 @@ def tune(dtype="bf16", target_nnz=16_000_000, seed=100, verbose=True):
                 for k, v in sorted(best.items())},
             "entries": dict(sorted(entries.items(), key=lambda kv: tuple(
                 int(t) for t in kv[0].split(","))))}
+
+
+def mixed_batch(dtype, seed=5, count=4096, device=None):
+    """The batched benchmark's generator (4096 matrices, rows log-uniform in
+    [64, 65536], log-normal row lengths with mean 8 and sigma 1) with another
+    seed; 16-bit values and per-row scales quantized in one array each at the
+    indices' offsets.  Returns (items, tensors to keep alive)."""
+    dev = device or torch.device("cuda", torch.cuda.current_device())
+    R, offc, idxc, valc, xc, rs, ns = synth.batched(count=count, seed=seed, device=dev)
+    items, y = api.batched_items(R, offc, idxc, valc, xc, rs, ns)
+    if dtype == "f32":
+        return items, (offc, idxc, valc, xc, y)
+    tdt = torch.bfloat16 if dtype == "bf16" else torch.float16
+    goff, gidx = synth.batch_as_one_csr(R, offc, idxc, rs, ns)
+    Q = api.CSR(goff, gidx, valc, goff.numel() - 1, goff.numel() - 1).quantized(
+        tdt, per_row_scale=True)
+    o = goff.cpu().numpy()
+    out = []
+    for m, (r, r0, n0) in enumerate(zip(R.tolist(), rs.tolist(), ns.tolist())):
+        nn = int(o[r0 + r] - o[r0])
+        out.append((api.CSR(offc[r0 + m: r0 + m + r + 1], idxc[n0: n0 + nn],
+                            Q.values[n0: n0 + nn], r, r, row_scale=Q.row_scale[r0: r0 + r]),
+                    xc[r0: r0 + r], y[r0: r0 + r]))
+    return out, (offc, idxc, valc, xc, y, Q)
+
+
+def validate(entries, dtype, verbose=True, gain=0.01):
+    """Keeps, row bucket by row bucket, the candidate entries that make the
+    mixed batch at least `gain` faster; returns (kept entries, log)."""
+    items, tensors = mixed_batch(dtype)
+    keep_alive = (items, tensors)
+    arr = api.batch_item_array(items)
+    flush = torch.empty((512 << 20) // 4, device=torch.device("cuda", torch.cuda.current_device()))
+
+    def t_of(ent):
+        plan = api.BatchPlan.from_array(arr, len(items), keep_alive,
+                                        table=api.tuning_table(ent) if ent else None)
+        ms = time_plan(plan, flush, reps=7)
+        plan.close()
+        return ms
+
+    kept = {}
+    best = t_of(kept)
+    log = [{"row_bucket": None, "ms": round(best, 5), "kept": True}]
+    for rb in sorted({int(k.split(",")[0]) for k in entries}):
+        trial = dict(kept)
+        trial.update({k: v for k, v in entries.items() if int(k.split(",")[0]) == rb})
+        ms = t_of(trial)
+        ok = ms <= (1.0 - gain) * best
+        log.append({"row_bucket": rb, "ms": round(ms, 5), "kept": ok})
+        if verbose:
+            print(f"validation: row bucket {rb}: {ms:.4f} ms against {best:.4f} ms "
+                  f"-> {'kept' if ok else 'dropped'}", flush=True)
+        if ok:
+            kept, best = trial, ms
+    full = t_of(entries) if entries else best
+    log.append({"row_bucket": "all candidates", "ms": round(full, 5), "kept": False})
+    return kept, log
 
 
 def dumps(table):
@@ -207,9 +269,12 @@ def main():
     if not torch.cuda.is_available():
         raise SystemExit("the tuner times kernels: it needs a GPU")
     table = tune(args.dtype, args.target_nnz)
+    table["candidates"] = table["entries"]
+    table["entries"], table["validation"] = validate(table["candidates"], args.dtype)
     with open(args.out, "w") as f:
         f.write(dumps(table))
-    print(f"wrote {len(table['entries'])} entries to {args.out}")
+    print(f"wrote {len(table['entries'])} of {len(table['candidates'])} candidate entries "
+          f"to {args.out}")
 
 
 if __name__ == "__main__":
