@@ -66,3 +66,24 @@ def test_batch_buckets_and_table_text():
     table = {"threads_per_row": [1, 2], "entries": {"3,4,1": [64, 12], "0,1,0": [4, 10]},
              "note": "x"}
     assert json.loads(tb.dumps(table)) == table
+
+
+def test_plan_default_table_is_the_validated_one():
+    """The plan's default table is what the tuner's validation on a mixed
+    batch kept (the recorded GB300 run kept no entry, so none is shipped
+    and the built-in rule applies to every bucket)."""
+    import os
+    from conftest import REPO
+    from edge_loops_gb300 import api
+    rec = json.load(open(os.path.join(REPO, "tests", "data", "batch_tuning_gb300_bf16.json")))
+    assert rec["validation"][0]["row_bucket"] is None  # the built-in rule's time comes first
+    kept = {k: v for k, v in rec["entries"].items()}
+    shipped = api.load_tuning_table()
+    if kept:
+        np.testing.assert_array_equal(shipped, api.tuning_table(kept))
+    else:
+        assert shipped is None
+    # every recorded step that dropped a row bucket's candidates was not faster by 1 %
+    base = rec["validation"][0]["ms"]
+    for step in rec["validation"][1:-1]:
+        assert step["kept"] or step["ms"] > 0.99 * base
