@@ -236,6 +236,8 @@ def run_ours(args, rank, world):
         opts["variant"] = args.variant
     if args.row_weight:
         opts["row_weight"] = args.row_weight
+    if args.nz_per_lane:
+        opts["nz_per_lane"] = args.nz_per_lane
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
 
@@ -1075,6 +1077,8 @@ def main():
                     help="merge_path kernel: 0 warp-streaming, 1 CTA ring")
     ap.add_argument("--row-weight", type=int, default=0,
                     help="merge_path: merge items per row end in the warp split (0 = default)")
+    ap.add_argument("--nz-per-lane", type=int, default=0, choices=[0, 8, 16],
+                    help="merge_path: nonzeros per lane of the tile walk (0 = the library's choice)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-row-scale", action="store_true",
                     help="16-bit values without per-row scales")

@@ -76,7 +76,8 @@ class ElSpmvOpts(C.Structure):
         ("test_hooks", C.c_int32),
         ("variant", C.c_int32),
         ("row_weight", C.c_int32),
-        ("reserved", C.c_int32 * 4),
+        ("nz_per_lane", C.c_int32),
+        ("reserved", C.c_int32 * 3),
     ]
 
 

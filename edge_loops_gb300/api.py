@@ -196,7 +196,7 @@ def workspace_errors(ws=None, clear=True, stream=None):
 
 def make_opts(threads_per_block=0, items_per_thread=0, threads_per_row=0, group_rows=0,
               num_threads=0, compensated=False, max_ctas=0, wait_limit_us=0, variant=0,
-              row_weight=0):
+              row_weight=0, nz_per_lane=0):
     o = L.ElSpmvOpts()
     L.lib().el_spmv_opts_default(C.byref(o))
     o.threads_per_block = threads_per_block
@@ -209,6 +209,7 @@ def make_opts(threads_per_block=0, items_per_thread=0, threads_per_row=0, group_
     o.wait_limit_us = wait_limit_us
     o.variant = variant
     o.row_weight = row_weight
+    o.nz_per_lane = nz_per_lane
     return o
 
 

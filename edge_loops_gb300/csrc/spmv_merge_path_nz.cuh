@@ -28,12 +28,18 @@
 namespace el {
 namespace mpn {
 
-constexpr int kPer = 8;               // nonzeros per lane: 8 or 16
-constexpr int kPerLog = kPer == 16 ? 4 : 3;
-constexpr int kTileNz = 32 * kPer;    // nonzeros per tile
+constexpr int kPer = 8;               // nonzeros per lane of the default tile (8 or 16)
+constexpr int kTileNz = 32 * kPer;    // nonzeros per default tile; range lengths are
+                                      // multiples of it whatever the tile
 constexpr int kMaxEnds = 256;         // row ends per tile (tiles are cut short
                                       // after this many, e.g. empty rows)
-constexpr int kStage = kTileNz > kMaxEnds ? kTileNz : kMaxEnds;  // staging slots per warp
+// The tile of KP nonzeros per lane (KP = 8 or 16, chosen per call).
+template <int KP>
+struct Geom {
+  static constexpr int log = KP == 16 ? 4 : 3;
+  static constexpr int tile = 32 * KP;
+  static constexpr int stage = tile > kMaxEnds ? tile : kMaxEnds;  // staging slots per warp
+};
 constexpr int kWarps = 8;
 constexpr int kTPB = 32 * kWarps;
 
@@ -57,28 +63,31 @@ struct Args {
   long long trace_cap;    // ranges the trace holds
 };
 
-template <bool COMP>
+template <bool COMP, int KP = kPer>
 struct __align__(16) WarpSmem {
-  int re[kMaxEnds];            // end position (tile-local nonzero index) of each row end
-  float yv[kStage];            // the tile's row sums (or, whole tiles, sums by end position)
-  float yc[COMP ? kStage : 4];
-  unsigned char kp[32][kPer];  // row end closed after lane l's product i (tile-local)
-  unsigned mw[32];             // whole tiles: bit i of word l = a row ends after nonzero kPer l + i
+  int re[kMaxEnds];                       // end position (tile-local nonzero index) of each row end
+  float yv[Geom<KP>::stage];              // the tile's row sums (or, whole tiles, by end position)
+  float yc[COMP ? Geom<KP>::stage : 4];
+  unsigned char kp[32][KP];               // row end closed after lane l's product i (tile-local)
+  unsigned mw[32];                        // whole tiles: bit i of word l = a row ends after
+                                          // nonzero KP l + i
   int pend;
   float pend_s, pend_c;
 };
 
-// kPer consecutive FP32 values (16-byte aligned: 128-bit loads).
-__device__ __forceinline__ void load8(const float* p, float (&v)[kPer]) {
+// KP consecutive FP32 values (16-byte aligned: 128-bit loads).
+template <int KP>
+__device__ __forceinline__ void load8(const float* p, float (&v)[KP]) {
 #pragma unroll
-  for (int k = 0; k < kPer / 4; ++k) {
+  for (int k = 0; k < KP / 4; ++k) {
     const float4 a = __ldcs(reinterpret_cast<const float4*>(p) + k);
     v[4 * k] = a.x; v[4 * k + 1] = a.y; v[4 * k + 2] = a.z; v[4 * k + 3] = a.w;
   }
 }
-__device__ __forceinline__ void load8i(const int* p, int (&c)[kPer]) {
+template <int KP>
+__device__ __forceinline__ void load8i(const int* p, int (&c)[KP]) {
 #pragma unroll
-  for (int k = 0; k < kPer / 4; ++k) {
+  for (int k = 0; k < KP / 4; ++k) {
     const int4 a = __ldcs(reinterpret_cast<const int4*>(p) + k);
     c[4 * k] = a.x; c[4 * k + 1] = a.y; c[4 * k + 2] = a.z; c[4 * k + 3] = a.w;
   }
@@ -92,20 +101,20 @@ __device__ __forceinline__ float ld_val(const VT* p) {
 // A lane's 8 values of the tile in flight.  16-bit values stay packed as
 // loaded (4 words) and are widened only when the products are formed, so no
 // instruction waits on the load before then.
-template <typename VT>
+template <typename VT, int KP = kPer>
 struct TileVals {
-  float v[kPer];
+  float v[KP];
   __device__ __forceinline__ void load_vec(const float* p) { load8(p, v); }
   __device__ __forceinline__ void load_at(int i, const float* p) { v[i] = ld_val(p); }
   __device__ __forceinline__ void zero_at(int i) { v[i] = 0.f; }
   __device__ __forceinline__ float get(int i) const { return v[i]; }
 };
-template <typename H>
+template <typename H, int KP>
 struct TileVals16 {
-  uint32_t w[kPer / 2];
+  uint32_t w[KP / 2];
   __device__ __forceinline__ void load_vec(const H* p) {
 #pragma unroll
-    for (int k = 0; k < kPer / 8; ++k) {
+    for (int k = 0; k < KP / 8; ++k) {
       const uint4 u = __ldcs(reinterpret_cast<const uint4*>(p) + k);
       w[4 * k] = u.x; w[4 * k + 1] = u.y; w[4 * k + 2] = u.z; w[4 * k + 3] = u.w;
     }
@@ -122,16 +131,16 @@ struct TileVals16 {
     return (unsigned short)((i & 1) ? (w[i >> 1] >> 16) : (w[i >> 1] & 0xffffu));
   }
 };
-template <>
-struct TileVals<__nv_bfloat16> : TileVals16<__nv_bfloat16> {
+template <int KP>
+struct TileVals<__nv_bfloat16, KP> : TileVals16<__nv_bfloat16, KP> {
   __device__ __forceinline__ float get(int i) const {
-    return __uint_as_float((uint32_t)half_at(i) << 16);
+    return __uint_as_float((uint32_t)this->half_at(i) << 16);
   }
 };
-template <>
-struct TileVals<__half> : TileVals16<__half> {
+template <int KP>
+struct TileVals<__half, KP> : TileVals16<__half, KP> {
   __device__ __forceinline__ float get(int i) const {
-    return __half2float(__ushort_as_half(half_at(i)));
+    return __half2float(__ushort_as_half(this->half_at(i)));
   }
 };
 
@@ -147,19 +156,19 @@ struct Src {
   unsigned cols;
   int nnz;
   int vec_ok;  // 128-bit loads allowed at tile starts
-  int ph;      // tiles start where (nonzero index + ph) is a multiple of kTileNz
+  int ph;      // tiles start where (nonzero index + ph) is a multiple of the tile size
 };
 
 // 128-bit loads of indices and values need both arrays at the same phase
 // modulo 8 elements (indices 4-byte, values element-aligned); tiles then
 // start on 32-byte boundaries of both.  Otherwise every load is scalar.
 inline void tile_phase(const void* indices, const void* values, int vbytes, int* vec_ok,
-                       int* ph) {
+                       int* ph, int tile = kTileNz) {
   const uintptr_t ia = (uintptr_t)indices, va = (uintptr_t)values;
   const bool ok = ia % 4 == 0 && va % (uintptr_t)vbytes == 0 &&
                   ((ia / 4) - (va / (uintptr_t)vbytes)) % 8 == 0;
   *vec_ok = ok ? 1 : 0;
-  *ph = ok ? (int)((ia / 4) % kTileNz) : 0;
+  *ph = ok ? (int)((ia / 4) % (uintptr_t)tile) : 0;
 }
 
 // The warp walks the merge range from (rs, ns) to (re, ne): rows [rs, re)
@@ -168,11 +177,14 @@ inline void tile_phase(const void* indices, const void* values, int vbytes, int*
 // partial sum of the row still open at the end (row re's nonzeros [.., ne))
 // is returned.  Sets bad / bad_col on malformed input; ra_out = the first
 // row not closed.
-template <typename VT, bool COMP>
-__device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, const int lane,
+template <typename VT, bool COMP, int KP = kPer>
+__device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP, KP>& S, const int lane,
                                                const int rs, const int re, const int ns,
                                                const int ne, const bool need_lb, bool& bad,
                                                bool& bad_col, int& ra_out) {
+  constexpr int kPer = KP;  // this walk's tile: KP nonzeros per lane
+  constexpr int kPerLog = Geom<KP>::log;
+  constexpr int kTileNz = Geom<KP>::tile;
   const VT* vals = reinterpret_cast<const VT*>(m.values);
   const float* __restrict__ scale = m.row_scale;
   const int rows = m.rows;
@@ -185,7 +197,7 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
     return t < (unsigned)ne ? (int)t : ne;
   };
   int c[kPer];
-  TileVals<VT> v;
+  TileVals<VT, KP> v;
   auto load_tile = [&](int l, int h) {
     const int j0 = l + kPer * lane;
     if (m.vec_ok && h - l == kTileNz && ((l + m.ph) & 7) == 0) {
@@ -480,14 +492,16 @@ __device__ __forceinline__ Acc<COMP> walk_rows(const Src& m, WarpSmem<COMP>& S, 
 }
 
 // The walk of this file as a policy of run_range.
-struct NzWalk {
+template <int KP>
+struct NzWalkK {
   template <typename VT, bool COMP, typename SmemT>
   static __device__ __forceinline__ Acc<COMP> walk(const Src& m, SmemT& S, int lane, int rs,
                                                    int re, int ns, int ne, bool need_lb,
                                                    bool& bad, bool& bad_col, int& ra) {
-    return walk_rows<VT, COMP>(m, S, lane, rs, re, ns, ne, need_lb, bad, bad_col, ra);
+    return walk_rows<VT, COMP, KP>(m, S, lane, rs, re, ns, ne, need_lb, bad, bad_col, ra);
   }
 };
+using NzWalk = NzWalkK<kPer>;
 
 // One warp's merge range, shared by the merge-path kernels: takes a range
 // id from the ticket, finds its split points, walks it with `Walk`
@@ -631,11 +645,11 @@ __device__ __forceinline__ void run_range(const Args& a, SmemT& S, const int war
 
 }
 
-template <typename VT, bool COMP>
-__global__ void __launch_bounds__(kTPB, kPer == 16 ? 2 : 3)
+template <typename VT, bool COMP, int KP = kPer>
+__global__ void __launch_bounds__(kTPB, KP == 16 ? 2 : 3)
     merge_path_nz_kernel(const Args a) {
-  __shared__ WarpSmem<COMP> smem_all[kWarps];
-  run_range<VT, COMP, NzWalk>(a, smem_all[threadIdx.x >> 5], kWarps);
+  __shared__ WarpSmem<COMP, KP> smem_all[kWarps];
+  run_range<VT, COMP, NzWalkK<KP>>(a, smem_all[threadIdx.x >> 5], kWarps);
 }
 
 // Merge items per row end for the warp ranges: a row end costs the walk
@@ -650,20 +664,45 @@ inline int row_weight(const SpmvCall& c) {
   return w;
 }
 
-template <typename VT, bool COMP>
+template <typename VT, bool COMP, int KP = kPer>
 int resident_warps(int device) {
   const int per_sm =
-      resident_ctas_per_sm((const void*)merge_path_nz_kernel<VT, COMP>, kTPB, 0);
+      resident_ctas_per_sm((const void*)merge_path_nz_kernel<VT, COMP, KP>, kTPB, 0);
   return (per_sm > 0 ? per_sm : 1) * kWarps * device_info(device).sm_count;
 }
 
+// Nonzeros per lane of the tile walk: opts.nz_per_lane (8 or 16), else 16
+// for 16-bit values on matrices with long rows (at least kLongRows nonzeros
+// per row on average and at least 2^20 nonzeros), 8 otherwise.  A 512-nonzero
+// tile halves the per-nonzero cost of the row-end ballot, scan and store,
+// which binds 16-bit values on banded matrices, but its registers allow
+// only two CTAs per SM, which costs more than it saves where the x gathers
+// or short rows bind.
+constexpr long long kLongRows = 24;
+inline int nz_per_lane(const SpmvCall& c, int vbytes) {
+  if (c.o.nz_per_lane == 8 || c.o.nz_per_lane == 16) return c.o.nz_per_lane;
+  const bool long_rows = c.A.nnz >= kLongRows * c.A.rows && c.A.nnz >= (1LL << 20);
+  return vbytes == 2 && long_rows ? 16 : 8;
+}
+
+template <typename VT, bool COMP, int KP>
+el_status launch_kp(const SpmvCall& c);
+
 template <typename VT, bool COMP>
 el_status launch(const SpmvCall& c) {
+  if (c.o.nz_per_lane != 0 && c.o.nz_per_lane != 8 && c.o.nz_per_lane != 16)
+    return fail(EL_ERR_INVALID_ARGUMENT, "nz_per_lane must be 0, 8 or 16");
+  return nz_per_lane(c, (int)sizeof(VT)) == 16 ? launch_kp<VT, COMP, 16>(c)
+                                               : launch_kp<VT, COMP, 8>(c);
+}
+
+template <typename VT, bool COMP, int KP>
+el_status launch_kp(const SpmvCall& c) {
   const int rw = row_weight(c);
   const long long total = (long long)rw * c.A.rows + c.A.nnz;
   // ranges of whole 256-item units, one per resident warp
   const long long units = (total + kTileNz - 1) / kTileNz;
-  long long W = resident_warps<VT, COMP>(c.device);
+  long long W = resident_warps<VT, COMP, KP>(c.device);
   if (c.o.max_ctas > 0 && (long long)c.o.max_ctas * kWarps < W) W = (long long)c.o.max_ctas * kWarps;
   if (W > units) W = units;
   if (W < 1) W = 1;
@@ -680,7 +719,7 @@ el_status launch(const SpmvCall& c) {
   a.y = c.y;
   a.range_items = upr * kTileNz;
   a.num_ranges = (units + upr - 1) / upr;
-  tile_phase(c.A.indices, c.A.values, (int)sizeof(VT), &a.vec_ok, &a.ph);
+  tile_phase(c.A.indices, c.A.values, (int)sizeof(VT), &a.vec_ok, &a.ph, Geom<KP>::tile);
   a.rw = rw;
   a.test_hooks = c.o.test_hooks;
   a.wait_ns = c.wait_ns;
@@ -690,13 +729,15 @@ el_status launch(const SpmvCall& c) {
   if (a.num_ranges > c.ws.nslots)
     return fail(EL_ERR_INVALID_ARGUMENT, "merge_path: workspace too small");
   const long long grid = (a.num_ranges + kWarps - 1) / kWarps;
-  merge_path_nz_kernel<VT, COMP><<<(unsigned)grid, kTPB, 0, c.stream>>>(a);
+  merge_path_nz_kernel<VT, COMP, KP><<<(unsigned)grid, kTPB, 0, c.stream>>>(a);
   return cuda_status(cudaGetLastError(), "merge_path launch");
 }
 
 template <typename VT, bool COMP>
 long long slots_needed(const SpmvCall& c) {
-  return resident_warps<VT, COMP>(c.device);
+  const long long a = resident_warps<VT, COMP, 8>(c.device);
+  const long long b = resident_warps<VT, COMP, 16>(c.device);
+  return a > b ? a : b;
 }
 
 }  // namespace mpn

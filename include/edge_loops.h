@@ -175,7 +175,13 @@ typedef struct el_spmv_opts {
                                 ranges of short rows hold fewer items; 0 =
                                 the library default, 1 = the reference's
                                 equal split */
-  int32_t reserved[4];
+  int32_t nz_per_lane;       /* merge_path (variant 0): nonzeros per lane of the
+                                tile walk, 8 (tiles of 256) or 16 (tiles of 512);
+                                0 = 16 for 16-bit values on matrices with at
+                                least 24 nonzeros per row on average and 2^20
+                                nonzeros in all, else 8.  Same results within
+                                the FP32 bound (the summation order changes) */
+  int32_t reserved[3];
 } el_spmv_opts;
 
 typedef struct el_workspace el_workspace;

@@ -138,3 +138,17 @@ def test_static_scratch_range_splits(cuda, oracle_mod, name):
         if ranges:
             assert len(tr) <= ranges
         _check(oracle_mod, off, tr, 1)
+
+
+@pytest.mark.parametrize("name", ["random3", "power_law"])
+def test_range_splits_with_512_nonzero_tiles(cuda, oracle_mod, name):
+    """Tiles of 16 nonzeros per lane walk the same ranges."""
+    from edge_loops_gb300 import api
+    off, idx, vals, cols = _case(name)
+    A = api.CSR.from_arrays(off, idx, vals, cols, device=cuda)
+    x = torch.rand(cols, device=cuda)
+    for w in (1, 2):
+        tr = _trace_run(lambda: api.spmv(A, x, schedule="merge_path_flat", row_weight=w,
+                                         nz_per_lane=16), 1 << 14, cuda)
+        _check(oracle_mod, off, tr, w)
+    assert api.workspace_errors() == 0

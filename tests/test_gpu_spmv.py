@@ -18,6 +18,9 @@ SCHEDS = [
     ("merge_path_flat", {"compensated": True}),
     ("merge_path_flat", {"row_weight": 1}),
     ("merge_path_flat", {"row_weight": 5, "max_ctas": 3}),
+    ("merge_path_flat", {"nz_per_lane": 16}),
+    ("merge_path_flat", {"nz_per_lane": 16, "compensated": True}),
+    ("merge_path_flat", {"nz_per_lane": 16, "max_ctas": 2}),
     ("merge_path_flat", {"variant": 2}),
     ("merge_path_flat", {"variant": 2, "compensated": True}),
     ("merge_path_flat", {"variant": 1}),
@@ -148,7 +151,8 @@ def test_edge_cases(cuda, oracle_mod, sched, opts):
         check_against_oracle(oracle_mod, off, idx, vals, x, y)
 
 
-@pytest.mark.parametrize("opts", [{}, {"compensated": True}, {"variant": 2}, {"max_ctas": 2}])
+@pytest.mark.parametrize("opts", [{}, {"compensated": True}, {"variant": 2}, {"max_ctas": 2},
+                                  {"nz_per_lane": 16}])
 @pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
 def test_merge_path_unaligned_arrays(cuda, oracle_mod, opts, dtype):
     """indices and values starting at every phase modulo 8 elements, equal
