@@ -7,12 +7,14 @@
 // global diagonals g * range_items, every warp taking one range (id from an
 // atomic ticket, so a range only ever waits on ranges already running), so
 // every warp gets the same number of rows + nonzeros.  Inside its range a
-// warp walks TILES OF 256 NONZEROS (aligned to multiples of 256), lane l
-// owning the 8 consecutive nonzeros 8l..8l+7 of the tile:
+// warp walks TILES OF 32 KP NONZEROS (aligned to multiples of the tile),
+// lane l owning the KP consecutive nonzeros KP l .. KP l + KP - 1 of the
+// tile; KP = 8 (tiles of 256) by default, 16 (tiles of 512) for 16-bit
+// values on long rows (nz_per_lane):
 //
-//   * a lane loads its 8 column indices and 8 values with 128-bit vector
+//   * a lane loads its KP column indices and KP values with 128-bit vector
 //     loads straight into registers (the next tile's loads are issued while
-//     the current tile reduces), gathers x and forms 8 products;
+//     the current tile reduces), gathers x and forms KP products;
 //   * the rows that end inside the tile come from a window of row offsets
 //     (one ballot per 32 rows) as a sorted list of end positions in shared
 //     memory; a lane adds its products in order and closes a row whenever
