@@ -18,9 +18,13 @@ every step.  The metric is achieved bandwidth in GB/s of the algorithmic
 with host buffers, the H2D copy of the matrix and x (pinned memory) and the
 D2H copy of y inside the timed region (row blocks of --e2e-block-nnz
 nonzeros, default the library's); `graph_replay` times 100 SpMVs captured
-in one CUDA graph and replayed without L2 flushes between them.  `--impl reference` times the
-reference's CPU SpMV loop (examples/spmv/helpers.hxx:106-112, restated in
-oracle/oracle.c, rows split over every host core) on the same workload.
+in one CUDA graph and replayed without L2 flushes between them; `secondary`
+measures the 27-point stencil (FP32, BF16, FP16) and the 4096-matrix batch in
+the same run.  Every output is checked against an FP64 evaluation.
+`--impl reference` times the reference's CPU SpMV loop
+(examples/spmv/helpers.hxx:106-112, restated in oracle/oracle.c, rows split
+over every host core) on the same workload, and the reference's own
+merge_path_flat CUDA kernel where its cubin was built.
 
 Under torchrun with N > 1 every rank runs an independent replica (SpMV of
 one matrix does not shard on this pool); value is the sum over ranks.
