@@ -352,9 +352,10 @@ def run_secondary(args, dev):
     """The other configurations of the target, measured in the same run as
     the headline (same timing rules: L2 flushed before every step, outside
     the CUDA events): the 27-point stencil on 160^3 with FP32, BF16 and FP16
-    values (16-bit with per-row scales), and the 4096-matrix batch
+    values (16-bit with per-row scales), the 4096-matrix batch
     (measure_batched: BF16 and FP32 plans and the plain FP32 kernel once per
-    matrix).  Every output is checked against FP64."""
+    matrix), and the SpMM on the ~8M-nonzero power-law matrix at n = 32 and
+    128 (FP32 and BF16 B).  Every output is checked against FP64."""
     import numpy as np
     import torch
     from edge_loops_gb300 import api, synth
@@ -410,6 +411,21 @@ def run_secondary(args, dev):
         b[dt]["frac"] = round(b[dt]["GBps"] / peak, 4)
         b[dt]["traffic"] = traffic_for(f"spmv_batched:{dt}")
     out["batched4096"] = b
+    torch.cuda.empty_cache()
+
+    A = spmm_matrix(dev)
+    sp = {"workload": "SpMM C = A B, A power-law 2^20 x 2^20 ~8M nnz (Zipf 2.0, cap 1e5, seed 3), "
+                      "B 2^20 x n uniform [-1, 1]; merge_path; GB/s of the compulsory bytes "
+                      "(A + B + C once), the gather model (a B row per nonzero) beside it"}
+    for n, bdt in ((32, "f32"), (128, "f32"), (128, "bf16")):
+        r = measure_spmm(A, n, bdt, "merge_path_flat", steps, warm, flush, stream)
+        sp[f"n{n}_{bdt}"] = {"ms": round(r["ms"], 4), "GBps": round(r["GBps"], 1),
+                             "frac": round(r["GBps"] / peak, 4),
+                             "GBps_gather_model": round(r["GBps_gather_model"], 1),
+                             "entries_outside_fp32_bound_of_2048_rows": r["entries_outside_fp32_bound"],
+                             "traffic": traffic_for(f"spmm_powerlaw:merge_path_flat:{bdt}:{n}")}
+    out["spmm_powerlaw8M"] = sp
+    del A
     torch.cuda.empty_cache()
     return out
 
@@ -738,43 +754,47 @@ def _time_device(step, steps, warmup, flush, stream):
     return sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / steps
 
 
-def run_spmm(args):
-    """SpMM C = A B (the SpMM workload): A power-law 2^20 x 2^20 with ~8M
-    nonzeros (Zipf 2.0, cap 100000, seed 3), B dense row-major 2^20 x n."""
-    import numpy as np
-    import torch
+def spmm_matrix(dev):
+    """The SpMM workload's A: power-law 2^20 x 2^20 with ~8M nonzeros (Zipf
+    2.0, cap 100000, seed 3)."""
     from edge_loops_gb300 import api, synth
-    dev = torch.device("cuda", 0)
-    torch.cuda.set_device(dev)
     off, idx, vals, x, cols = synth.power_law(rows=1 << 20, target_nnz=8_000_000, exponent=2.0,
                                               cap=100_000, seed=3, device=dev)
-    A = api.CSR(off, idx, vals, off.numel() - 1, cols)
+    return api.CSR(off, idx, vals, off.numel() - 1, cols)
+
+
+def measure_spmm(A, n, b_dtype, schedule, steps, warmup, flush, stream):
+    """C = A B with B dense row-major cols x n (uniform [-1, 1], seed 33) of
+    b_dtype: time per step (L2 flushed before each, outside the events),
+    compulsory bytes (A + B + C once) and the gather model (A + a B row per
+    nonzero + C), checked on 2048 sampled rows of C against FP64."""
+    import numpy as np
+    import torch
+    from edge_loops_gb300 import api
+    dev = A.device
     g = torch.Generator(device=dev)
     g.manual_seed(33)
-    B = torch.rand(cols, args.n, generator=g, device=dev) * 2 - 1
-    bdt = {"f32": torch.float32, "bf16": torch.bfloat16, "f16": torch.float16}[args.b_dtype]
-    B = B.to(bdt)
-    Cm = torch.empty(A.rows, args.n, device=dev)
+    B = torch.rand(A.cols, n, generator=g, device=dev) * 2 - 1
+    B = B.to({"f32": torch.float32, "bf16": torch.bfloat16, "f16": torch.float16}[b_dtype])
+    Cm = torch.empty(A.rows, n, device=dev)
     sb = B.element_size()
-    compulsory = A.nnz * 8 + 4 * (A.rows + 1) + cols * args.n * sb + A.rows * args.n * 4
-    gather = A.nnz * 8 + 4 * (A.rows + 1) + A.nnz * args.n * sb + A.rows * args.n * 4
+    compulsory = A.nnz * 8 + 4 * (A.rows + 1) + A.cols * n * sb + A.rows * n * 4
+    gather = A.nnz * 8 + 4 * (A.rows + 1) + A.nnz * n * sb + A.rows * n * 4
     ws = api.Workspace()
-    flush = torch.empty(L2_FLUSH_BYTES // 4, device=dev)
-    ms = _time_device(lambda: api.spmm(A, B, Cm, schedule=args.schedule, workspace=ws),
-                      args.steps, args.warmup, flush, torch.cuda.current_stream())
+    ms = _time_device(lambda: api.spmm(A, B, Cm, schedule=schedule, workspace=ws),
+                      steps, warmup, flush, stream)
     if ws.errors():
         raise SystemExit("device error flags in SpMM")
-    # parity on a sample of 2048 rows: FP64 of those rows
     rng = np.random.default_rng(0)
     rows_s = np.sort(rng.choice(A.rows, 2048, replace=False))
-    offh, idxh, valh = off.cpu().numpy(), idx.cpu().numpy(), vals.cpu().numpy()
+    offh, idxh, valh = (t.cpu().numpy() for t in (A.offsets, A.indices, A.values))
     lens = offh[rows_s + 1] - offh[rows_s]
     sel = np.concatenate([np.arange(offh[r], offh[r + 1]) for r in rows_s])
     row_of = np.repeat(np.arange(len(rows_s)), lens)
     Bh = B.float().cpu().numpy()
     prod = valh[sel].astype(np.float64)[:, None] * Bh[idxh[sel]].astype(np.float64)
-    C64 = np.zeros((len(rows_s), args.n))
-    Ca = np.zeros((len(rows_s), args.n))
+    C64 = np.zeros((len(rows_s), n))
+    Ca = np.zeros((len(rows_s), n))
     np.add.at(C64, row_of, prod)
     np.add.at(Ca, row_of, np.abs(prod))
     got = Cm[torch.as_tensor(rows_s, device=dev)].cpu().numpy().astype(np.float64)
@@ -782,8 +802,24 @@ def run_spmm(args):
     bad = int(np.sum(np.abs(got - C64) > fp32_bound(so, 1.0)[:, None] * Ca))
     if bad:
         raise SystemExit(f"SpMM output fails the FP64 bound in {bad} entries")
+    return {"ms": ms, "compulsory_bytes": compulsory, "gather_model_bytes": gather,
+            "GBps": compulsory / (ms * 1e-3) / 1e9,
+            "GBps_gather_model": gather / (ms * 1e-3) / 1e9, "sampled_rows": 2048,
+            "entries_outside_fp32_bound": bad}
+
+
+def run_spmm(args):
+    """SpMM C = A B (the SpMM workload): A power-law 2^20 x 2^20 with ~8M
+    nonzeros (Zipf 2.0, cap 100000, seed 3), B dense row-major 2^20 x n."""
+    import torch
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    A = spmm_matrix(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, device=dev)
+    r = measure_spmm(A, args.n, args.b_dtype, args.schedule, args.steps, args.warmup, flush,
+                     torch.cuda.current_stream())
+    ms, ach = r["ms"], r["GBps"]
     peak, kind = measured_peaks()
-    ach = compulsory / (ms * 1e-3) / 1e9
     return {
         "metric": "SpMM achieved bandwidth (compulsory bytes / kernel time)",
         "value": round(ach, 2), "unit": "GB/s", "n_gpus": 1, "steps": args.steps,
@@ -794,11 +830,12 @@ def run_spmm(args):
         "config": {"workload": "SpMM power-law 2^20 x 2^20 ~8M nnz (Zipf 2.0, cap 1e5, seed 3),"
                                f" B 2^20 x {args.n} {args.b_dtype}",
                    "schedule": args.schedule, "n": args.n, "nnz": A.nnz,
-                   "compulsory_bytes": compulsory, "gather_model_bytes": gather,
+                   "compulsory_bytes": r["compulsory_bytes"],
+                   "gather_model_bytes": r["gather_model_bytes"],
                    "l2": "flushed before every step (512 MiB write, outside the timed kernel)"},
         "roofline": {"bound": "hbm", "achieved": round(ach, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(ach / peak, 4), "peak_source": kind,
-                     "achieved_gather_model": round(gather / (ms * 1e-3) / 1e9, 2),
+                     "achieved_gather_model": round(r["GBps_gather_model"], 2),
                      "traffic": traffic_for(f"spmm_powerlaw:{args.schedule}:{args.b_dtype}:{args.n}")},
         "gpu_launches": args.steps * ((args.n + 127) // 128),
         "check": {"sampled_rows": 2048, "entries_outside_fp32_bound": 0},
