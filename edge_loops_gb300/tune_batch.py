@@ -206,28 +206,18 @@ def mixed_batch(dtype, seed=5, count=4096, device=None):
     return out, (offc, idxc, valc, xc, y, Q)
 
 
-def validate(entries, dtype, verbose=True, gain=0.01):
-    """Keeps, row bucket by row bucket, the candidate entries that make the
-    mixed batch at least `gain` faster; returns (kept entries, log)."""
-    items, tensors = mixed_batch(dtype)
-    keep_alive = (items, tensors)
-    arr = api.batch_item_array(items)
-    flush = torch.empty((512 << 20) // 4, device=torch.device("cuda", torch.cuda.current_device()))
-
-    def t_of(ent):
-        plan = api.BatchPlan.from_array(arr, len(items), keep_alive,
-                                        table=api.tuning_table(ent) if ent else None)
-        ms = time_plan(plan, flush, reps=7)
-        plan.close()
-        return ms
-
+def select_entries(entries, time_of, gain=0.01, verbose=False):
+    """Greedy validation: starting from the built-in rule (no entries), add
+    the candidate entries of one row bucket at a time (ascending) and keep
+    them only if time_of(table entries) drops by at least `gain`.  Returns
+    (kept entries, log of every step, the last with all candidates)."""
     kept = {}
-    best = t_of(kept)
+    best = time_of(kept)
     log = [{"row_bucket": None, "ms": round(best, 5), "kept": True}]
     for rb in sorted({int(k.split(",")[0]) for k in entries}):
         trial = dict(kept)
         trial.update({k: v for k, v in entries.items() if int(k.split(",")[0]) == rb})
-        ms = t_of(trial)
+        ms = time_of(trial)
         ok = ms <= (1.0 - gain) * best
         log.append({"row_bucket": rb, "ms": round(ms, 5), "kept": ok})
         if verbose:
@@ -235,9 +225,27 @@ def validate(entries, dtype, verbose=True, gain=0.01):
                   f"-> {'kept' if ok else 'dropped'}", flush=True)
         if ok:
             kept, best = trial, ms
-    full = t_of(entries) if entries else best
+    full = time_of(entries) if entries else best
     log.append({"row_bucket": "all candidates", "ms": round(full, 5), "kept": False})
     return kept, log
+
+
+def validate(entries, dtype, verbose=True, gain=0.01):
+    """select_entries with the time of the mixed batch (mixed_batch) under
+    each table."""
+    items, tensors = mixed_batch(dtype)
+    keep_alive = (items, tensors)
+    arr = api.batch_item_array(items)
+    flush = torch.empty((512 << 20) // 4, device=torch.device("cuda", torch.cuda.current_device()))
+
+    def time_of(ent):
+        plan = api.BatchPlan.from_array(arr, len(items), keep_alive,
+                                        table=api.tuning_table(ent) if ent else None)
+        ms = time_plan(plan, flush, reps=7)
+        plan.close()
+        return ms
+
+    return select_entries(entries, time_of, gain, verbose)
 
 
 def dumps(table):

@@ -87,3 +87,27 @@ def test_plan_default_table_is_the_validated_one():
     base = rec["validation"][0]["ms"]
     for step in rec["validation"][1:-1]:
         assert step["kept"] or step["ms"] > 0.99 * base
+
+
+def test_validation_keeps_only_row_buckets_that_speed_up_the_batch():
+    """The tuner's greedy validation on a fake batch timer: a row bucket's
+    candidates stay only when the batch gets >= 1 % faster with them on top
+    of those already kept; the log ends with all candidates together."""
+    from edge_loops_gb300 import tune_batch as tb
+    entries = {"3,2,0": [4, 11], "3,3,1": [64, 10], "8,4,0": [64, 11], "12,5,2": [1, 12],
+               "14,1,0": [32, 13]}
+    effect = {3: -0.05, 8: +0.02, 12: -0.004, 14: -0.03}  # relative change per row bucket
+
+    def time_of(ent):
+        t = 1.0
+        for rb in {int(k.split(",")[0]) for k in ent}:
+            t *= 1.0 + effect[rb]
+        return t
+
+    kept, log = tb.select_entries(entries, time_of)
+    assert set(kept) == {"3,2,0", "3,3,1", "14,1,0"}
+    assert [s["row_bucket"] for s in log] == [None, 3, 8, 12, 14, "all candidates"]
+    assert [s["kept"] for s in log[1:-1]] == [True, False, False, True]
+    assert log[-1]["ms"] == pytest.approx(0.95 * 1.02 * 0.996 * 0.97, abs=1e-5)
+    assert tb.select_entries({}, time_of) == ({}, [log[0], {"row_bucket": "all candidates",
+                                                           "ms": 1.0, "kept": False}])
