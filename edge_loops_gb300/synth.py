@@ -48,12 +48,22 @@ def _sorted_distinct_columns(lens, off, cols, g, device):
 
 def uniform_rows(rows=1000, cols=1000, per_row=10, seed=0, device="cpu"):
     """Every row has exactly `per_row` nonzeros in distinct uniformly drawn
-    columns (sorted); values and x uniform in [-1, 1]."""
+    columns (sorted); values and x uniform in [-1, 1].
+
+    Up to 2^24 cells the columns are the `per_row` smallest keys of a dense
+    rows x cols uniform draw (the draw the committed fixtures were made
+    with); larger shapes draw them per row without the dense matrix."""
+    if per_row > cols:
+        raise ValueError(f"per_row={per_row} exceeds cols={cols}")
     g = _gen(seed, device)
-    keys = torch.rand(rows, cols, generator=g, device=device)
-    idx = torch.topk(keys, per_row, dim=1, largest=False).indices
-    idx, _ = torch.sort(idx, dim=1)
     off = torch.arange(0, rows * per_row + 1, per_row, device=device, dtype=torch.int64)
+    if rows * cols <= (1 << 24):
+        keys = torch.rand(rows, cols, generator=g, device=device)
+        idx = torch.topk(keys, per_row, dim=1, largest=False).indices
+        idx, _ = torch.sort(idx, dim=1)
+    else:
+        lens = torch.full((rows,), per_row, device=device, dtype=torch.int64)
+        idx = _sorted_distinct_columns(lens, off, cols, g, device)
     vals = _uniform(rows * per_row, -1.0, 1.0, g, device)
     x = _uniform(cols, -1.0, 1.0, g, device)
     return off.to(torch.int32), idx.reshape(-1).to(torch.int32), vals, x, cols

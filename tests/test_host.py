@@ -138,6 +138,12 @@ def test_generators():
     assert float(val.min()) >= -1 and float(val.max()) <= 1
     off2, idx2, *_ = synth.uniform_rows(seed=0)
     assert torch.equal(idx, idx2)
+    # Above 2^24 cells the columns are drawn per row: no rows x cols matrix.
+    off, idx, val, x, cols = synth.uniform_rows(rows=1 << 13, cols=1 << 12, per_row=7, seed=2)
+    assert int(off[-1]) == 7 << 13 and int(idx.min()) >= 0 and int(idx.max()) < cols
+    assert bool((idx.view(-1, 7).diff(dim=1) > 0).all())
+    with pytest.raises(ValueError):
+        synth.uniform_rows(rows=4, cols=3, per_row=4)
     off, idx, val, x, cols = synth.power_law(rows=1 << 12, target_nnz=60_000, cap=3000, seed=1)
     lens = off.long().diff()
     assert int(lens.min()) >= 1 and int(lens.max()) <= 3000
