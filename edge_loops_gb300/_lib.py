@@ -102,6 +102,7 @@ class ElRowStats(C.Structure):
         ("empty_rows", C.c_int64),
         ("mean_row_nnz", C.c_double),
         ("cv", C.c_double),
+        ("coherence", C.c_double),
     ]
 
 
@@ -188,6 +189,9 @@ SIGNATURES = {
     "el_select_schedule": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, C.c_int64,
                                      C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                      C.POINTER(C.c_double)]),
+    "el_select_schedule_stats": (C.c_int, [C.c_int64, C.c_int64, C.c_int64,
+                                           C.POINTER(ElRowStats), C.POINTER(C.c_int32),
+                                           C.POINTER(ElSpmvOpts), C.POINTER(C.c_double)]),
     "el_spmv_select": (C.c_int, [C.c_void_p, C.POINTER(ElCsr), C.POINTER(C.c_int32),
                                  C.POINTER(ElSpmvOpts), C.c_void_p]),
     "el_debug_range_trace": (C.c_int, [C.c_void_p, C.c_int64]),

@@ -230,13 +230,15 @@ def spmv(A, x, y=None, schedule="merge_path_flat", stream=None, workspace=None, 
 
 def row_stats(A, stream=None, workspace=None):
     """el_csr_row_stats: longest row, empty rows, mean row length and its
-    coefficient of variation (synchronises the stream)."""
+    coefficient of variation, and the row-to-row coherence of the columns
+    (synchronises the stream)."""
     st = L.ElRowStats()
     a = A.el()
     L.check(L.lib().el_csr_row_stats(_ws(workspace), C.byref(a), C.byref(st), _stream(stream)),
             "el_csr_row_stats")
     return {"max_row_nnz": int(st.max_row_nnz), "empty_rows": int(st.empty_rows),
-            "mean_row_nnz": float(st.mean_row_nnz), "cv": float(st.cv)}
+            "mean_row_nnz": float(st.mean_row_nnz), "cv": float(st.cv),
+            "coherence": float(st.coherence)}
 
 
 def select_schedule(A, stream=None, workspace=None):
@@ -248,7 +250,10 @@ def select_schedule(A, stream=None, workspace=None):
     L.check(L.lib().el_spmv_select(_ws(workspace), C.byref(a), C.byref(sched), C.byref(o),
                                    _stream(stream)), "el_spmv_select")
     if sched.value == L.EL_SCHED_THREAD_MAPPED:
-        return "thread_mapped", {"threads_per_row": int(o.threads_per_row)}
+        opts = {"threads_per_row": int(o.threads_per_row)}
+        if o.variant:
+            opts["variant"] = int(o.variant)  # rows staged through shared memory
+        return "thread_mapped", opts
     return "merge_path_flat", {}
 
 

@@ -74,8 +74,38 @@ struct SpmvImpl {
     thread_mapped_spmv_kernel<VT, TPR, COMP><<<(unsigned)grid, tpb, 0, c.stream>>>(basic(c));
     return cuda_status(cudaGetLastError(), "thread_mapped launch");
   }
+  // One lane per row, rows staged through shared memory (indices and values
+  // 16-byte aligned): a grid of every resident CTA at most, each warp
+  // striding over chunks of 32 rows.
+  template <bool COMP>
+  static el_status tm_staged(const SpmvCall& c) {
+    using S = TmStage<VT>;
+    auto kern = thread_mapped_staged_kernel<VT, COMP>;
+    static int attr_done[64] = {0};
+    if (c.device >= 0 && c.device < 64 && !attr_done[c.device]) {
+      cudaError_t e =
+          cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S::kSmem);
+      if (e != cudaSuccess) return cuda_status(e, "thread_mapped smem attribute");
+      attr_done[c.device] = 1;
+    }
+    const int per_sm = resident_ctas_per_sm((const void*)kern, 32 * S::kWarps, S::kSmem);
+    if (per_sm < 1) return fail(EL_ERR_CUDA, "thread_mapped: staged kernel does not fit on an SM");
+    const long long chunks = (c.A.rows + 31) / 32;
+    long long grid = (chunks + S::kWarps - 1) / S::kWarps;
+    const long long cap = c.o.max_ctas > 0 ? (long long)c.o.max_ctas
+                                           : (long long)device_info(c.device).sm_count * per_sm;
+    if (grid > cap) grid = cap;
+    if (grid < 1) grid = 1;
+    kern<<<(unsigned)grid, 32 * S::kWarps, S::kSmem, c.stream>>>(basic(c));
+    return cuda_status(cudaGetLastError(), "thread_mapped launch");
+  }
   template <bool COMP>
   static el_status tm_tpr(const SpmvCall& c) {
+    if (c.o.variant != 0 && c.o.variant != 1)
+      return fail(EL_ERR_INVALID_ARGUMENT, "thread_mapped variant must be 0 or 1");
+    // variant 1: one lane per row, rows staged through shared memory
+    const bool aligned = ((uintptr_t)c.A.indices % 16 == 0) && ((uintptr_t)c.A.values % 16 == 0);
+    if (c.o.variant == 1 && c.o.threads_per_row <= 1 && aligned) return tm_staged<COMP>(c);
     switch (c.o.threads_per_row) {
       case 0:
       case 1: return tm<1, COMP>(c);

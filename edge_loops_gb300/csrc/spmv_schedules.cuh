@@ -145,6 +145,207 @@ __global__ void __launch_bounds__(256, 5)
   }
 }
 
+// ------------------------------------------------- thread_mapped, staged
+// The same schedule and summation order as thread_mapped_spmv_kernel with
+// one lane per row (y bit-identical to it), for matrices whose rows are
+// short: read straight from the CSR arrays, lane l's index and value loads
+// stride by its row length, so each load instruction touches 32 lines.
+// Here a warp copies the indices and values of its chunk of 32 rows into
+// shared memory with coalesced 16-byte asynchronous copies (two buffers per
+// warp: the next chunk is in flight while this one is summed), and each lane
+// then walks its row from there.  The x gathers keep the row-aligned order
+// (lane l reads x near row r0 + l), which on banded matrices puts a gather
+// instruction's 32 addresses on one or two lines.  Warp gw takes chunks
+// gw, gw + nw, gw + 2 nw, ... (nw warps in the grid).
+//
+// A chunk whose nonzeros do not fit a buffer of CAP (long rows), or whose
+// offsets fail the range checks, is summed straight from global memory as
+// the unstaged kernel does, in its turn.  Every chunk fits when no row holds
+// more than kStagedMaxRow nonzeros, which is when el_spmv_select picks this
+// kernel.  Requires indices and values 16-byte aligned (checked by the
+// launcher).
+template <typename VT>
+struct TmStage {
+  static constexpr int kCap = 880;   // nonzeros per buffer
+  static constexpr int kWarps = 4;   // per CTA: 4 CTAs of FP32 buffers per SM
+  static constexpr int kIdxBytes = kCap * 4;
+  static constexpr int kValBytes = (kCap * (int)sizeof(VT) + 15) / 16 * 16;
+  static constexpr int kBuf = kIdxBytes + kValBytes;
+  static constexpr int kSmem = kWarps * 2 * kBuf;
+  static constexpr int kValPerUnit = 16 / (int)sizeof(VT);
+  static constexpr int kBatch = 16;  // nonzeros of a row gathered together
+};
+// 32 rows of this many nonzeros, their start rounded down to 16 bytes, fit.
+constexpr int kStagedMaxRow = 27;
+static_assert(((32 * kStagedMaxRow + 3 + 3) / 4) * 16 <= TmStage<float>::kIdxBytes, "cap");
+static_assert(((32 * kStagedMaxRow + 7 + 7) / 8) * 16 <= TmStage<__nv_bfloat16>::kValBytes,
+              "cap");
+
+// A lane's row in one chunk: raw offsets (checked when staged) and its
+// scale, loaded a chunk ahead.
+struct TmRows {
+  int lo, hi;
+  float scale;
+};
+
+// One row summed straight from global memory (the unstaged kernel's walk).
+template <typename VT, bool COMP>
+__device__ __forceinline__ void tm_direct_row(const BasicArgs& a, long long row) {
+  Acc<COMP> acc;
+  bool bad = false;
+  long long b, e;
+  row_bounds(a, row, &b, &e);
+  accumulate<VT, 1, COMP, 8>(a, b, e, acc, bad);
+  if (bad) raise_flag(a.hdr, EL_FLAG_INDEX_RANGE, (unsigned)row);
+  a.y[row] = scaled(a, row, acc.value());
+}
+
+template <typename VT, bool COMP>
+__global__ void __launch_bounds__(32 * TmStage<VT>::kWarps)
+    thread_mapped_staged_kernel(const BasicArgs a) {
+  using S = TmStage<VT>;
+  constexpr int W = S::kBatch;
+  extern __shared__ __align__(16) unsigned char tm_smem[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned char* const wbase = tm_smem + (size_t)w * 2 * S::kBuf;
+  const long long nchunks = (a.rows + 31) >> 5;
+  const long long nw = (long long)gridDim.x * S::kWarps;
+  long long q = (long long)blockIdx.x * S::kWarps + w;
+  const VT* __restrict__ gvals = reinterpret_cast<const VT*>(a.values);
+
+  auto load_rows = [&](long long qq) {
+    TmRows r{0, 0, 1.f};
+    const long long row = (qq << 5) + lane;
+    if (qq < nchunks && row < a.rows) {
+      r.lo = __ldg(a.offsets + row);
+      r.hi = __ldg(a.offsets + row + 1);
+      if (a.row_scale) r.scale = __ldg(a.row_scale + row);
+    }
+    return r;
+  };
+  // Chunk qq, ahead of its turn: staged into buffer `buf` (returns the
+  // staged extent's start in indices, rounded down to 16 bytes) or left to
+  // be summed from global memory (-1; also past the last chunk).  Always
+  // commits one copy group.
+  auto stage = [&](long long qq, const TmRows& r, int buf) {
+    int ai = -1;
+    if (qq < nchunks) {
+      const long long r0 = qq << 5;
+      const int last = (int)((a.rows - r0 < 32 ? a.rows - r0 : 32) - 1);
+      const bool mine = lane <= last;
+      const int b0 = __shfl_sync(kFullMask, r.lo, 0);
+      const int e0 = __shfl_sync(kFullMask, r.hi, last);
+      const bool ok = !mine || (r.lo >= b0 && r.lo <= r.hi && r.hi <= e0);
+      const int i0 = b0 & ~3;
+      const int v0 = b0 & ~(S::kValPerUnit - 1);
+      // copy units (16 bytes) of each array, checked against the buffers
+      const long long ni = ((long long)e0 - i0 + 3) >> 2;
+      const long long nv = ((long long)e0 - v0 + S::kValPerUnit - 1) / S::kValPerUnit;
+      const bool fits = a.cols > 0 && b0 >= 0 && e0 <= a.nnz && b0 <= e0 &&
+                        ni * 16 <= S::kIdxBytes && nv * 16 <= S::kValBytes;
+      if (__all_sync(kFullMask, ok) && fits) {
+        ai = i0;
+        unsigned char* const dst = wbase + (size_t)buf * S::kBuf;
+        // whole 16-byte units; the array's last partial unit, when the chunk
+        // reaches it, is zero-filled past the end
+        const int* const gi = a.indices + i0;
+        const int fi = (int)(ni < ((a.nnz - i0) >> 2) ? ni : ((a.nnz - i0) >> 2));
+        for (int u = lane; u < fi; u += 32) cp_async16(dst + 16 * u, gi + 4 * u, 16);
+        if (fi < ni && lane == 0)
+          cp_async16(dst + 16 * fi, gi + 4 * fi, (int)(a.nnz - i0 - 4LL * fi) * 4);
+        const VT* const gv = gvals + v0;
+        const long long vleft = (a.nnz - v0) / S::kValPerUnit;
+        const int fv = (int)(nv < vleft ? nv : vleft);
+        for (int u = lane; u < fv; u += 32)
+          cp_async16(dst + S::kIdxBytes + 16 * u, gv + S::kValPerUnit * u, 16);
+        if (fv < nv && lane == 0)
+          cp_async16(dst + S::kIdxBytes + 16 * fv, gv + S::kValPerUnit * fv,
+                     (int)((a.nnz - v0 - (long long)S::kValPerUnit * fv) * (long long)sizeof(VT)));
+      }
+    }
+    cp_async_commit();
+    return ai;
+  };
+
+  TmRows cur = load_rows(q);
+  int cst = stage(q, cur, 0);
+  TmRows nxt = load_rows(q + nw);
+  int buf = 0;
+  for (; q < nchunks; q += nw) {
+    const int nst = stage(q + nw, nxt, buf ^ 1);
+    const TmRows nn = load_rows(q + 2 * nw);
+    cp_async_wait<1>();
+    __syncwarp();
+    const long long row = (q << 5) + lane;
+    const bool has_row = row < a.rows;
+    if (cst >= 0) {
+      const unsigned char* const src = wbase + (size_t)buf * S::kBuf;
+      const int av = cst & ~(S::kValPerUnit - 1);
+      const int* __restrict__ si = reinterpret_cast<const int*>(src) + (cur.lo - cst);
+      const VT* __restrict__ sv =
+          reinterpret_cast<const VT*>(src + S::kIdxBytes) + (cur.lo - av);
+      const int n = has_row ? cur.hi - cur.lo : 0;
+      // Gathers use the column clamped to [0, cols); a row with a column out
+      // of range is summed again by the unstaged walk, which skips those
+      // nonzeros and raises the flag.
+      const unsigned lastc = (unsigned)(a.cols - 1);
+      unsigned cmax = 0;
+      Acc<COMP> acc;
+      int j0 = 0;
+      // whole batches of W: no per-nonzero predicates
+      for (; j0 + W <= n; j0 += W) {
+        int c[W];
+        float v[W], xv[W];
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+          c[k] = si[j0 + k];
+          v[k] = to_f32(sv[j0 + k]);
+        }
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+          cmax = max(cmax, (unsigned)c[k]);
+          xv[k] = __ldg(a.x + min((unsigned)c[k], lastc));
+        }
+#pragma unroll
+        for (int k = 0; k < W; ++k) acc.add(__fmul_rn(v[k], xv[k]));
+      }
+      // the rest, predicated per nonzero
+      if (j0 < n) {
+        int c[W];
+        float v[W], xv[W];
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+          const bool t = j0 + k < n;
+          c[k] = t ? si[j0 + k] : 0;
+          v[k] = t ? to_f32(sv[j0 + k]) : 0.f;
+        }
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+          cmax = max(cmax, (unsigned)c[k]);
+          xv[k] = j0 + k < n ? __ldg(a.x + min((unsigned)c[k], lastc)) : 0.f;
+        }
+#pragma unroll
+        for (int k = 0; k < W; ++k)
+          if (j0 + k < n) acc.add(__fmul_rn(v[k], xv[k]));
+      }
+      if (has_row) {
+        if (cmax > lastc)
+          tm_direct_row<VT, COMP>(a, row);
+        else
+          a.y[row] = a.row_scale ? acc.value() * cur.scale : acc.value();
+      }
+    } else if (has_row) {
+      tm_direct_row<VT, COMP>(a, row);
+    }
+    __syncwarp();  // the buffer is free before it is staged into again
+    cur = nxt;
+    nxt = nn;
+    cst = nst;
+    buf ^= 1;
+  }
+  cp_async_wait<0>();
+}
+
 // ------------------------------------------------------------- group_mapped
 // The reference's group_mapped schedule [include/loops/schedule/
 // group_mapped.hxx:146-235, include/loops/algorithms/spmv/group_mapped.cuh:

@@ -41,7 +41,8 @@
  * and adds entry points the reference does not have: el_spmv_host (matrix,
  * x and y in host memory, streamed), el_spmv_static_scratch (no device
  * allocation), the batched plan (el_batch_plan_*), schedule selection
- * (el_spmv_select, el_select_schedule, el_csr_row_stats),
+ * (el_spmv_select, el_select_schedule, el_select_schedule_stats,
+ * el_csr_row_stats),
  * el_quantize_values and el_csr_validate.  include/edge_loops_device.cuh holds the device-side
  * load-balanced loop API for user kernels (the reference's schedule::setup).
  *
@@ -168,7 +169,22 @@ typedef struct el_spmv_opts {
                                 2 = warp ranges walked in tiles of 256 merge
                                     items, lane t from the split point of
                                     diagonal 8t (the reference's per-thread
-                                    split) */
+                                    split).
+                                thread_mapped with one lane per row (y
+                                bit-identical either way):
+                                0 = each lane reads its row straight from
+                                    the CSR arrays;
+                                1 = a warp copies its 32 rows' indices and
+                                    values into shared memory (coalesced
+                                    asynchronous copies, the next 32 rows in
+                                    flight) and each lane walks its row from
+                                    there: faster on short rows (the whole
+                                    32-row chunk fits when no row holds more
+                                    than 27 nonzeros; a chunk that does not
+                                    is read as in 0, in its turn, which makes
+                                    long rows slower than in 0).  Needs 16-byte
+                                    aligned indices and values, else 0 runs.
+                                    el_spmv_select sets it where it pays. */
   int32_t row_weight;        /* merge_path (variant 0): the warp ranges split
                                 the merge of row ends and nonzeros with a
                                 row end counted as this many nonzeros, so
@@ -342,7 +358,8 @@ el_status el_spmv_edge(el_workspace* ws, const el_coo* A,
  * The predictor the reference's paper fits to its per-matrix timings
  * (plots/data/heuristics.csv), here a cost model of this library's kernels
  * on GB300: estimated times of merge_path and of thread_mapped with 1, 4
- * and 32 lanes per row from (rows, nnz, longest row).  EL_SCHED_AUTO in
+ * and 32 lanes per row from (rows, nnz, longest row), and with the row
+ * coherence also of one lane per row staged through shared memory.  EL_SCHED_AUTO in
  * el_spmv cannot see the longest row without a synchronisation, so it
  * applies the model with the longest row taken as nnz (the worst case):
  * merge_path, the choice that is never far off, except for matrices of a
@@ -353,20 +370,32 @@ typedef struct el_row_stats {
   int64_t max_row_nnz;
   int64_t empty_rows;
   double mean_row_nnz;
-  double cv; /* standard deviation / mean of the row lengths */
+  double cv;        /* standard deviation / mean of the row lengths */
+  double coherence; /* new: on about 2^16 sampled rows r, the fraction of the
+                       first (up to 32) column pairs (col(r, j), col(r+1, j))
+                       that step by 0, 1 or 2 -- near 1 on banded and stencil
+                       matrices, near 0 on scattered columns */
 } el_row_stats;
 
 /* Row statistics of A's offsets (one kernel; synchronises `stream`). */
 el_status el_csr_row_stats(el_workspace* ws, const el_csr* A, el_row_stats* out,
                            el_stream_t stream);
-/* The cost model: schedule (EL_SCHED_MERGE_PATH_FLAT or
- * EL_SCHED_THREAD_MAPPED), lanes per row for thread_mapped (else 0), and
- * the estimated time in microseconds (may be NULL).  Host only. */
+/* The cost model without the coherence (the staged kernel is not weighed):
+ * schedule (EL_SCHED_MERGE_PATH_FLAT or EL_SCHED_THREAD_MAPPED), lanes per
+ * row for thread_mapped (else 0), and the estimated time in microseconds
+ * (may be NULL).  Host only. */
 el_status el_select_schedule(int64_t rows, int64_t cols, int64_t nnz,
                              int64_t max_row_nnz, int32_t* schedule,
                              int32_t* threads_per_row, double* est_us);
-/* el_csr_row_stats + el_select_schedule: writes the schedule, and for
- * thread_mapped opts->threads_per_row (other fields are left alone). */
+/* The cost model with all of el_row_stats: also weighs thread_mapped's
+ * staged kernel (variant 1), where no row holds more than 27 nonzeros and
+ * the coherence is at least 0.5.  Writes the schedule and, for
+ * thread_mapped, opts->threads_per_row and opts->variant (other fields are
+ * left alone).  Host only. */
+el_status el_select_schedule_stats(int64_t rows, int64_t cols, int64_t nnz,
+                                   const el_row_stats* stats, int32_t* schedule,
+                                   el_spmv_opts* opts, double* est_us);
+/* el_csr_row_stats + el_select_schedule_stats. */
 el_status el_spmv_select(el_workspace* ws, const el_csr* A, int32_t* schedule,
                          el_spmv_opts* opts, el_stream_t stream);
 

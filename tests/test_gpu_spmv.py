@@ -1,7 +1,8 @@
 """GPU parity of the SpMV path against the oracle, through the C ABI.
 
 Bars: split points bit-identical to the restated reference search; the
-TPR=1 thread_mapped schedule bit-identical to the reference CPU loop; every
+TPR=1 thread_mapped schedule (both kernels) bit-identical to the reference
+CPU loop; every
 schedule within the order-free FP32 bound gamma_(n+2) * sum|a x| of the FP64
 oracle (valid for any summation order) and within the reference's own
 |gpu - cpu| <= 1e-2 check."""
@@ -32,6 +33,9 @@ SCHEDS = [
     ("thread_mapped", {"compensated": True}),
     ("thread_mapped", {"threads_per_row": 8}),
     ("thread_mapped", {"threads_per_row": 32}),
+    ("thread_mapped", {"variant": 1}),
+    ("thread_mapped", {"variant": 1, "compensated": True}),
+    ("thread_mapped", {"variant": 1, "max_ctas": 1}),
     ("group_mapped", {}),
     ("group_mapped", {"group_rows": 32}),
     ("group_mapped", {"threads_per_block": 256, "group_rows": 256}),
@@ -105,17 +109,55 @@ def _tm_cases():
 
 @pytest.mark.parametrize("case", ["random", "stencil24", "power_law", "row_lengths"])
 @pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
-def test_thread_mapped_bit_exact_with_reference_loop(cuda, oracle_mod, case, dtype):
-    """One lane per row: y is the reference CPU loop's, bit for bit (16-bit
+@pytest.mark.parametrize("variant", [0, 1])
+def test_thread_mapped_bit_exact_with_reference_loop(cuda, oracle_mod, case, dtype, variant):
+    """One lane per row, rows read in place (variant 0) or staged through
+    shared memory (1): y is the reference CPU loop's, bit for bit (16-bit
     values: the loop over their exact FP32 widening)."""
     (off, idx, vals, x), cols = next(c[1:] for c in _tm_cases() if c[0] == case)
     A = dev_csr(off, idx, vals, cols, cuda)
     if dtype != torch.float32:
         A = A.quantized(dtype, per_row_scale=False)
         vals = A.values.float().cpu().numpy()
-    y, flags = run(A, x, "thread_mapped", {}, cuda)
+    y, flags = run(A, x, "thread_mapped", {"variant": variant}, cuda)
     assert flags == 0
     np.testing.assert_array_equal(y, oracle_mod.spmv_f32(off, idx, vals, x))
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16, torch.float16])
+def test_thread_mapped_staged_equals_unstaged(cuda, dtype):
+    """The staged kernel (variant 1) against the unstaged one, bit for bit:
+    per-row scales, compensated sums, chunks that do not fit the buffer next
+    to ones that do, arrays whose ends fall inside a 16-byte copy unit, and
+    arrays not 16-byte aligned (the unstaged kernel runs)."""
+    from edge_loops_gb300 import api
+    rng = np.random.default_rng(61)
+    cases = [random_csr(rng, rows=rows, cols=700, max_len=ml, empty_frac=0.1, long_rows=lr)
+             for rows, ml, lr in [(1, 27, []), (31, 27, []), (33, 27, []), (4097, 27, []),
+                                  (2000, 9, [(5, 600), (1999, 40)]), (3001, 60, []),
+                                  (500, 1, [])]]
+    for off, idx, vals, x in cases:
+        nnz = len(idx)
+        xt = torch.as_tensor(x, device=cuda)
+        for shift in (0, 1, 4):  # 4 elements: still 16-byte aligned for FP32
+            ib = torch.zeros(nnz + 8, dtype=torch.int32, device=cuda)
+            vb = torch.zeros(nnz + 8, dtype=dtype, device=cuda)
+            ib[shift: shift + nnz] = torch.as_tensor(idx, device=cuda)
+            vb[shift: shift + nnz] = torch.as_tensor(vals).to(dtype).to(cuda)
+            scale = None if dtype == torch.float32 else \
+                torch.as_tensor(rng.uniform(0.5, 2.0, len(off) - 1).astype(np.float32),
+                                device=cuda)
+            A = api.CSR(torch.as_tensor(off, device=cuda), ib[shift: shift + nnz],
+                        vb[shift: shift + nnz], len(off) - 1, len(x), row_scale=scale)
+            for comp in (False, True):
+                ys = []
+                for variant in (0, 1):
+                    y = torch.full((A.rows,), float("nan"), device=cuda)
+                    api.spmv(A, xt, y, schedule="thread_mapped", variant=variant,
+                             compensated=comp)
+                    ys.append(y)
+                assert api.workspace_errors() == 0
+                assert torch.equal(ys[0], ys[1]), (len(off) - 1, shift, comp)
 
 
 def _power_law_case(cuda, rows=1 << 16, nnz=1_500_000, cap=40_000, seed=1):

@@ -3,10 +3,11 @@ nnz, longest row), a schedule whose measured time is close to the best one.
 
 CPU: the model's choices on the committed GB300 sweep
 (tests/data/select_sweep_gb300.csv, made by edge_loops_gb300/tune_select.py:
-every schedule timed on 119 synthetic shapes) are within 2 % of the best
+every schedule timed on 133 synthetic shapes) are within 2 % of the best
 per shape on geometric mean, never worse than 1.35x, and better than always
-running merge_path; argument errors.  GPU: row statistics equal numpy's,
-and the selected schedule's SpMV is within the FP32 bound.
+running merge_path; argument errors.  GPU: row statistics (with the row
+coherence) equal numpy's, and the selected schedule's SpMV is within the
+FP32 bound.
 """
 import csv
 import ctypes as C
@@ -29,23 +30,48 @@ def choose(L, rows, nnz, mx):
             est.value)
 
 
+def choose_stats(L, rows, nnz, mx, coh):
+    """el_select_schedule_stats: "tms" for thread_mapped's staged kernel."""
+    from edge_loops_gb300 import api
+    st = L.ElRowStats()
+    st.max_row_nnz, st.coherence = mx, coh
+    s, o, est = C.c_int32(), api.make_opts(), C.c_double()
+    assert L.lib().el_select_schedule_stats(rows, rows, nnz, C.byref(st), C.byref(s),
+                                            C.byref(o), C.byref(est)) == L.EL_OK
+    if s.value == L.EL_SCHED_MERGE_PATH_FLAT:
+        return "merge_path", est.value
+    return ("tms" if o.variant == 1 else "tm%d" % o.threads_per_row), est.value
+
+
 def test_model_quality_on_the_sweep(built_lib):
+    """Measured time of the chosen kernel over the best one per shape (the
+    staged kernel's time counts where it was measured: rows of at most 27
+    nonzeros, coherent or not)."""
     from edge_loops_gb300 import _lib as L
-    loss, loss_mp = [], []
+    loss, loss_mp, loss_plain = [], [], []
+    staged_picked = 0
     with open(SWEEP) as f:
         for r in csv.DictReader(f):
-            t = {c: float(r[c]) for c in CANDIDATES}
+            t = {c: float(r[c]) for c in CANDIDATES + ("tms",) if r[c] != ""}
             best = min(t.values())
-            c, est = choose(L, int(r["rows"]), int(r["nnz"]), int(r["max"]))
+            c, est = choose_stats(L, int(r["rows"]), int(r["nnz"]), int(r["max"]),
+                                  float(r["coherence"]))
             assert est > 0
+            staged_picked += c == "tms"
             loss.append(t[c] / best)
             loss_mp.append(t["merge_path"] / best)
+            # without the coherence the staged kernel is never picked
+            c0, _ = choose(L, int(r["rows"]), int(r["nnz"]), int(r["max"]))
+            assert c0 != "tms"
+            loss_plain.append(t[c0] / best)
     loss, loss_mp = np.array(loss), np.array(loss_mp)
     gm = float(np.exp(np.log(loss).mean()))
-    assert len(loss) >= 100
+    assert len(loss) >= 130
     assert gm <= 1.02, gm
     assert loss.max() <= 1.35, loss.max()
     assert gm < float(np.exp(np.log(loss_mp).mean())) - 0.2
+    assert staged_picked >= 3  # the larger stencils
+    assert gm <= float(np.exp(np.log(np.array(loss_plain)).mean()))
 
 
 def test_selection_rules_and_errors(built_lib):
@@ -79,6 +105,13 @@ def test_row_stats(cuda):
         assert st["mean_row_nnz"] == pytest.approx(lens.mean())
         cv = lens.std() / lens.mean() if lens.mean() > 0 else 0.0
         assert st["cv"] == pytest.approx(cv, rel=1e-6, abs=1e-9)
+        assert st["coherence"] == pytest.approx(coherence(off, idx), rel=1e-12, abs=1e-12)
+    # a stencil's consecutive rows repeat their pattern one column over
+    from edge_loops_gb300 import synth
+    o, i, v, x, n = synth.stencil27(n=20, seed=2)
+    st = api.row_stats(api.CSR.from_arrays(o, i, v, n, device="cuda"))
+    assert st["coherence"] == pytest.approx(coherence(o.numpy(), i.numpy()), rel=1e-12)
+    assert st["coherence"] > 0.8 and st["max_row_nnz"] == 27
 
 
 @pytest.mark.gpu
@@ -90,6 +123,7 @@ def test_select_then_spmv(cuda, oracle_mod):
     A = api.CSR.from_arrays(off, idx, vals, cols, device=dev)
     sched, o = api.select_schedule(A)
     assert sched == "thread_mapped" and o["threads_per_row"] in (1, 4, 32)
+    assert o.get("variant", 0) == 0  # scattered columns: the unstaged walk
     y = api.spmv(A, x.to(dev), schedule=sched, **o).cpu().numpy()
     on, ix, vv, xx = off.numpy(), idx.numpy(), vals.numpy(), x.numpy()
     y64, yabs = oracle_mod.spmv_f64(on, ix, vv, xx)
@@ -98,6 +132,15 @@ def test_select_then_spmv(cuda, oracle_mod):
                                               cap=60_000, seed=9)
     A = api.CSR.from_arrays(off, idx, vals, cols, device=dev)
     assert api.select_schedule(A) == ("merge_path_flat", {})
+    # a stencil: short coherent rows, the staged kernel, bit-identical to the
+    # reference CPU loop
+    off, idx, vals, x, n = synth.stencil27(n=100, seed=2)
+    A = api.CSR.from_arrays(off, idx, vals, n, device=dev)
+    sched, o = api.select_schedule(A)
+    assert (sched, o) == ("thread_mapped", {"threads_per_row": 1, "variant": 1})
+    y = api.spmv(A, x.to(dev), schedule=sched, **o).cpu().numpy()
+    np.testing.assert_array_equal(
+        y, oracle_mod.spmv_f32(off.numpy(), idx.numpy(), vals.numpy(), x.numpy()))
 
 
 @pytest.mark.gpu

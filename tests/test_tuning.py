@@ -8,21 +8,27 @@ import numpy as np
 import pytest
 
 
-def synthetic_sweep(consts, rng):
-    """Timings of the four candidates on random shapes, exactly as the cost
-    model with `consts` predicts them."""
+def synthetic_sweep(consts, rng, n=60):
+    """Timings of the candidates on random shapes, exactly as the cost model
+    with `consts` predicts them; the staged kernel ("tms", where consts has
+    it) is timed on short rows, as the model says where the rows are
+    coherent and three times slower where they are not."""
     data = []
-    for _ in range(60):
+    for _ in range(n):
         rows = int(2 ** rng.uniform(6, 22))
         per = float(2 ** rng.uniform(0, 8))
         nnz = int(rows * per)
         mx = int(min(nnz, per * 2 ** rng.uniform(0, 10)))
-        f = {"rows": rows, "nnz": nnz, "max": mx}
+        f = {"rows": rows, "nnz": nnz, "max": mx, "coh": float(rng.choice([0.0, 0.3, 0.9]))}
         a, e = consts["merge_path"]
         t = {"merge_path": a + e * (nnz + rows) / 1e6}
-        for tpr in (1, 4, 32):
-            a, c, d, e = consts["tm%d" % tpr]
-            t["tm%d" % tpr] = a + c * mx + d * rows / 1e3 + e * nnz / 1e6
+        for key in ("tm1", "tm4", "tm32", "tms"):
+            if key not in consts or (key == "tms" and mx > 27):
+                continue
+            a, c, d, e = consts[key]
+            t[key] = a + c * mx + d * rows / 1e3 + e * nnz / 1e6
+            if key == "tms" and f["coh"] < 0.5:
+                t[key] *= 3.0
         data.append(("synthetic", f, t))
     return data
 
@@ -41,6 +47,25 @@ def test_select_fit_recovers_a_known_model():
     assert q["shapes"] == len(data)
     # always merge_path is worse on this data, and quality says so
     assert ts.quality(data, lambda f: "merge_path")["geomean"] > 1.0
+
+
+def test_select_fit_of_the_staged_kernel_uses_only_the_shapes_it_applies_to():
+    pytest.importorskip("scipy")
+    from edge_loops_gb300 import tune_select as ts
+    consts = {"merge_path": (15.0, 4.0), "tm1": (7.0, 0.06, 0.004, 5.6),
+              "tm4": (6.7, 0.044, 0.026, 3.2), "tm32": (6.7, 0.007, 0.2, 1.8),
+              "tms": (6.6, 0.0, 0.02, 1.5)}
+    rng = np.random.default_rng(4)
+    # short rows, so that many shapes carry a staged timing
+    data = [d for d in synthetic_sweep(consts, rng, n=600) if d[1]["max"] <= 27][:80]
+    assert sum(ts.staged_applies(f) for _, f, _ in data) >= 10
+    assert any("tms" in t and not ts.staged_applies(f) for _, f, t in data)
+    model = ts.fit(data)
+    np.testing.assert_allclose(model["tms"], consts["tms"], rtol=1e-6, atol=1e-9)
+    q = ts.quality(data, lambda f: ts.predict(model, f))
+    assert q["geomean"] == pytest.approx(1.0) and q["worst"] == pytest.approx(1.0)
+    # never the staged kernel where it does not apply
+    assert all(ts.predict(model, f) != "tms" for _, f, _ in data if not ts.staged_applies(f))
 
 
 def test_select_predict_takes_the_cheapest_estimate():
