@@ -352,7 +352,8 @@ def run_secondary(args, dev):
     """The other configurations of the target, measured in the same run as
     the headline (same timing rules: L2 flushed before every step, outside
     the CUDA events): the 27-point stencil on 160^3 with FP32, BF16 and FP16
-    values (16-bit with per-row scales), the 4096-matrix batch
+    values (16-bit with per-row scales), with merge_path and with the schedule
+    el_spmv_select picks for it, the 4096-matrix batch
     (measure_batched: BF16 and FP32 plans and the plain FP32 kernel once per
     matrix), and the SpMM on the ~8M-nonzero power-law matrix at n = 32 and
     128 (FP32 and BF16 B).  Every output is checked against FP64."""
@@ -371,35 +372,53 @@ def run_secondary(args, dev):
     o, i, v, xh = (t.cpu().numpy() for t in (off, idx, vals, x))
     y64, yabs = fp64_spmv(o, i, v, xh)
     ws = api.Workspace()
+    # el_spmv_select's choice from the row statistics (the same for every
+    # value type): thread_mapped's staged kernel on these short coherent rows
+    sel_sched, sel_opts = api.select_schedule(A, workspace=ws)
     st = {"workload": "27-point stencil on 160^3 (4,096,000 rows, 109,215,352 nnz), diag 26.5, "
-                      "off-diag U[-1,0], x U[-1,1], seed 2; merge_path"}
+                      "off-diag U[-1,0], x U[-1,1], seed 2; merge_path, and under 'selected' "
+                      "the schedule el_spmv_select picks",
+          "selected_schedule": {"schedule": sel_sched, **sel_opts}}
     for dt in ("f32", "bf16", "f16"):
         Q = A if dt == "f32" else A.quantized(
             torch.bfloat16 if dt == "bf16" else torch.float16, per_row_scale=True)
-        y = torch.empty(rows, device=dev)
-        ms = _time_device(lambda: api.spmv(Q, x, y, workspace=ws), steps, warm, flush, stream)
-        if ws.errors():
-            raise SystemExit(f"device error flags in the stencil {dt} SpMV")
         nb = synth.algorithmic_bytes(rows, rows, Q.nnz, 4 if dt == "f32" else 2,
                                      row_scale=Q.row_scale is not None)
-        yy = y.cpu().numpy()
         if dt == "f32":
-            bad = int(np.sum(np.abs(yy - y64) > fp32_bound(o, yabs)))
+            q64, qabs = y64, yabs
         else:
             q64, qabs = fp64_spmv(o, i, Q.values.float().cpu().numpy(), xh,
                                   Q.row_scale.cpu().numpy())
+        for key, sched, opts in (("merge_path", "merge_path_flat", {}),
+                                 ("selected", sel_sched, sel_opts)):
+            y = torch.empty(rows, device=dev)
+            ms = _time_device(lambda: api.spmv(Q, x, y, schedule=sched, workspace=ws, **opts),
+                              steps, warm, flush, stream)
+            if ws.errors():
+                raise SystemExit(f"device error flags in the stencil {dt} SpMV ({key})")
+            yy = y.cpu().numpy()
             bad = int(np.sum(np.abs(yy - q64) > fp32_bound(o, qabs)))
-        comp, _ = rel_errors(yy, y64, yabs)
-        if bad or comp > 1e-2:
-            raise SystemExit(f"stencil {dt}: {bad} rows outside the FP32 bound, err {comp}")
-        gbps = nb / (ms * 1e-3) / 1e9
-        st[dt] = {"us": round(ms * 1e3, 2), "GBps": round(gbps, 1), "frac": round(gbps / peak, 4),
-                  "algorithmic_bytes": nb, "rows_outside_fp32_bound": bad,
-                  "max_rel_err_vs_fp64_of_fp32_matrix": comp,
-                  "traffic": traffic_for(f"spmv_stencil:merge_path_flat:{dt}")}
-        del Q, y
+            comp, _ = rel_errors(yy, y64, yabs)
+            if bad or comp > 1e-2:
+                raise SystemExit(f"stencil {dt} ({key}): {bad} rows outside the FP32 bound, "
+                                 f"err {comp}")
+            gbps = nb / (ms * 1e-3) / 1e9
+            r = {"us": round(ms * 1e3, 2), "GBps": round(gbps, 1),
+                 "frac": round(gbps / peak, 4), "algorithmic_bytes": nb,
+                 "rows_outside_fp32_bound": bad, "max_rel_err_vs_fp64_of_fp32_matrix": comp}
+            tkey = "merge_path_flat" if key == "merge_path" else \
+                sched + ("_staged" if opts.get("variant") == 1 else "")
+            r["traffic"] = traffic_for(f"spmv_stencil:{tkey}:{dt}")
+            if key == "merge_path":
+                st[dt] = r
+            else:
+                st[dt]["selected"] = r
+            del y
+        del Q
     for dt in ("bf16", "f16"):
         st[dt]["time_vs_f32"] = round(st[dt]["us"] / st["f32"]["us"], 4)
+        st[dt]["selected"]["time_vs_f32"] = round(
+            st[dt]["selected"]["us"] / st["f32"]["selected"]["us"], 4)
     out["stencil160"] = st
     del A, off, idx, vals, x, ws
     torch.cuda.empty_cache()

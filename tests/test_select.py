@@ -22,6 +22,25 @@ SWEEP = os.path.join(REPO, "tests", "data", "select_sweep_gb300.csv")
 CANDIDATES = ("merge_path", "tm1", "tm4", "tm32")
 
 
+def coherence(off, idx):
+    """el_row_stats.coherence restated: on every (rows >> 16)-th row r, the
+    first min(len r, len r+1, 32) column pairs of rows r and r+1 that step by
+    0, 1 or 2."""
+    rows = len(off) - 1
+    stride = max(1, rows >> 16)
+    off = off.astype(np.int64)
+    idx = idx.astype(np.int64)
+    pairs = steps = 0
+    for r in range(0, rows - 1, stride):
+        lo, hi, hi2 = off[r], off[r + 1], off[r + 2]
+        m = min(hi - lo, hi2 - hi, 32)
+        if m > 0:
+            d = idx[hi:hi + m] - idx[lo:lo + m]
+            steps += int(((d >= 0) & (d <= 2)).sum())
+            pairs += m
+    return steps / pairs if pairs else 0.0
+
+
 def choose(L, rows, nnz, mx):
     s, t, est = C.c_int32(), C.c_int32(), C.c_double()
     assert L.lib().el_select_schedule(rows, rows, nnz, mx, C.byref(s), C.byref(t),
