@@ -1,6 +1,7 @@
 """Parity at the benchmark sizes: the default merge-path SpMV on the 16M-
 nonzero power-law matrix and on the 109M-nonzero 27-point stencil (FP32, and
-BF16 and FP16 values with per-row scales), the merge-path and group_mapped
+BF16 and FP16 values with per-row scales), the schedule el_spmv_select picks
+for the stencil (bit for bit), the merge-path and group_mapped
 SpMM on the 8M-nonzero power-law matrix (n = 32 and 128, FP32 and BF16 B),
 and the batched plan over 4096 matrices (~310M nonzeros, FP32 and BF16),
 against the FP64 oracle.  Every output row is checked (the SpMM: 2048
@@ -70,6 +71,40 @@ def test_stencil160_f32_bf16_f16(cuda, oracle_mod):
         comp, _ = oracle_mod.error_metrics(yqh, y64, yabs)
         assert comp <= 1e-2, (dt, comp)
         del Q, yq, qv, sc, yqh
+
+
+def test_stencil160_selected_staged_thread_mapped(cuda, oracle_mod):
+    """The schedule el_spmv_select picks for the stencil (thread_mapped's
+    staged kernel): y is the reference CPU loop's bit for bit (FP32, and
+    BF16 values, whose loop runs on their exact FP32 widening), and the BF16
+    and FP16 runs with row scales agree bit for bit with the unstaged
+    kernel."""
+    from edge_loops_gb300 import api, synth
+    off, idx, vals, x, rows = synth.stencil27(n=160, seed=2, device=cuda)
+    A = api.CSR(off, idx, vals, rows, rows)
+    ws = api.Workspace()
+    sched, opts = api.select_schedule(A, workspace=ws)
+    assert (sched, opts) == ("thread_mapped", {"threads_per_row": 1, "variant": 1})
+    y = api.spmv(A, x, schedule=sched, workspace=ws, **opts)
+    torch.cuda.synchronize()
+    assert ws.errors() == 0
+    o, i, v, xh, yh = _host(off, idx, vals, x, y)
+    np.testing.assert_array_equal(yh, oracle_mod.spmv_f32(o, i, v, xh))
+    del y, yh
+    Q = A.quantized(torch.bfloat16, per_row_scale=False)
+    yq = api.spmv(Q, x, schedule=sched, workspace=ws, **opts)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(
+        yq.cpu().numpy(), oracle_mod.spmv_f32(o, i, Q.values.float().cpu().numpy(), xh))
+    del Q, yq
+    for dt in (torch.bfloat16, torch.float16):
+        Q = A.quantized(dt, per_row_scale=True)
+        ys = api.spmv(Q, x, schedule=sched, workspace=ws, **opts)
+        yu = api.spmv(Q, x, schedule="thread_mapped", workspace=ws)
+        torch.cuda.synchronize()
+        assert ws.errors() == 0
+        assert torch.equal(ys, yu), dt
+        del Q, ys, yu
 
 
 @pytest.mark.parametrize("n,bdt", [(32, torch.float32), (128, torch.float32),
