@@ -151,9 +151,10 @@ __global__ void __launch_bounds__(256, 5)
 // short: read straight from the CSR arrays, lane l's index and value loads
 // stride by its row length, so each load instruction touches 32 lines.
 // Here a warp copies the indices and values of its chunk of 32 rows into
-// shared memory with coalesced 16-byte asynchronous copies (two buffers per
-// warp: the next chunk is in flight while this one is summed), and each lane
-// then walks its row from there.  The x gathers keep the row-aligned order
+// shared memory with two bulk copies by the TMA engine (cp.async.bulk, one
+// mbarrier per buffer, L2 evict-first; two buffers per warp: the next chunk
+// is in flight while this one is summed), and each lane then walks its row
+// from there.  The x gathers keep the row-aligned order
 // (lane l reads x near row r0 + l), which on banded matrices puts a gather
 // instruction's 32 addresses on one or two lines.  Warp gw takes chunks
 // gw, gw + nw, gw + 2 nw, ... (nw warps in the grid).
@@ -206,8 +207,18 @@ __global__ void __launch_bounds__(32 * TmStage<VT>::kWarps)
   using S = TmStage<VT>;
   constexpr int W = S::kBatch;
   extern __shared__ __align__(16) unsigned char tm_smem[];
+  __shared__ __align__(8) uint64_t s_bar[S::kWarps][2];  // one per buffer
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   unsigned char* const wbase = tm_smem + (size_t)w * 2 * S::kBuf;
+  uint64_t pol = 0;  // the matrix streams: evict first, x keeps its L2 lines
+  uint32_t ph = 0;   // bit b: the parity of buffer b's next phase
+  if (lane == 0) {
+    mbar_init(&s_bar[w][0], 1);
+    mbar_init(&s_bar[w][1], 1);
+    fence_mbar_init();
+    pol = l2_policy_evict_first();
+  }
+  __syncwarp();
   const long long nchunks = (a.rows + 31) >> 5;
   const long long nw = (long long)gridDim.x * S::kWarps;
   long long q = (long long)blockIdx.x * S::kWarps + w;
@@ -225,8 +236,7 @@ __global__ void __launch_bounds__(32 * TmStage<VT>::kWarps)
   };
   // Chunk qq, ahead of its turn: staged into buffer `buf` (returns the
   // staged extent's start in indices, rounded down to 16 bytes) or left to
-  // be summed from global memory (-1; also past the last chunk).  Always
-  // commits one copy group.
+  // be summed from global memory (-1; also past the last chunk).
   auto stage = [&](long long qq, const TmRows& r, int buf) {
     int ai = -1;
     if (qq < nchunks) {
@@ -250,20 +260,24 @@ __global__ void __launch_bounds__(32 * TmStage<VT>::kWarps)
         // reaches it, is zero-filled past the end
         const int* const gi = a.indices + i0;
         const int fi = (int)(ni < ((a.nnz - i0) >> 2) ? ni : ((a.nnz - i0) >> 2));
-        for (int u = lane; u < fi; u += 32) cp_async16(dst + 16 * u, gi + 4 * u, 16);
-        if (fi < ni && lane == 0)
-          cp_async16(dst + 16 * fi, gi + 4 * fi, (int)(a.nnz - i0 - 4LL * fi) * 4);
         const VT* const gv = gvals + v0;
         const long long vleft = (a.nnz - v0) / S::kValPerUnit;
         const int fv = (int)(nv < vleft ? nv : vleft);
-        for (int u = lane; u < fv; u += 32)
-          cp_async16(dst + S::kIdxBytes + 16 * u, gv + S::kValPerUnit * u, 16);
-        if (fv < nv && lane == 0)
-          cp_async16(dst + S::kIdxBytes + 16 * fv, gv + S::kValPerUnit * fv,
-                     (int)((a.nnz - v0 - (long long)S::kValPerUnit * fv) * (long long)sizeof(VT)));
+        // two bulk copies by lane 0, completing on the buffer's barrier; the
+        // arrays' last partial units (the chunk that reaches their end) by
+        // plain loads
+        if (lane == 0) {
+          uint64_t* const bar = &s_bar[w][buf];
+          mbar_arrive_expect_tx(bar, 16u * (uint32_t)(fi + fv));
+          if (fi) bulk_g2s(dst, gi, 16u * fi, bar, pol);
+          if (fv) bulk_g2s(dst + S::kIdxBytes, gv, 16u * fv, bar, pol);
+          for (long long el = i0 + 4LL * fi; el < e0; ++el)
+            reinterpret_cast<int*>(dst)[el - i0] = __ldg(a.indices + el);
+          for (long long el = v0 + (long long)S::kValPerUnit * fv; el < e0; ++el)
+            reinterpret_cast<VT*>(dst + S::kIdxBytes)[el - v0] = gvals[el];
+        }
       }
     }
-    cp_async_commit();
     return ai;
   };
 
@@ -274,7 +288,13 @@ __global__ void __launch_bounds__(32 * TmStage<VT>::kWarps)
   for (; q < nchunks; q += nw) {
     const int nst = stage(q + nw, nxt, buf ^ 1);
     const TmRows nn = load_rows(q + 2 * nw);
-    cp_async_wait<1>();
+    if (cst >= 0) {
+      if (!mbar_wait_bounded(&s_bar[w][buf], (ph >> buf) & 1u, 2000000000ull)) {
+        if (lane == 0) raise_flag(a.hdr, EL_FLAG_TIMEOUT, (unsigned)q);
+        cst = -1;  // summed from global memory instead
+      }
+      ph ^= 1u << buf;
+    }
     __syncwarp();
     const long long row = (q << 5) + lane;
     const bool has_row = row < a.rows;
@@ -343,7 +363,6 @@ __global__ void __launch_bounds__(32 * TmStage<VT>::kWarps)
     cst = nst;
     buf ^= 1;
   }
-  cp_async_wait<0>();
 }
 
 // ------------------------------------------------------------- group_mapped

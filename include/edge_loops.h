@@ -175,9 +175,9 @@ typedef struct el_spmv_opts {
                                 0 = each lane reads its row straight from
                                     the CSR arrays;
                                 1 = a warp copies its 32 rows' indices and
-                                    values into shared memory (coalesced
-                                    asynchronous copies, the next 32 rows in
-                                    flight) and each lane walks its row from
+                                    values into shared memory (TMA bulk
+                                    copies, the next 32 rows in flight) and
+                                    each lane walks its row from
                                     there: faster on short rows (the whole
                                     32-row chunk fits when no row holds more
                                     than 27 nonzeros; a chunk that does not
