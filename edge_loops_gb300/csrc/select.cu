@@ -84,12 +84,12 @@ struct Cost {
   double a, c, d, e;  // a + c max_row + d rows/1e3 + e nnz/1e6 (us)
 };
 // merge_path: a + e (nnz + rows)/1e6 (c = d = 0)
-constexpr Cost kMergePath = {14.76, 0.0, 0.0, 3.503};
+constexpr Cost kMergePath = {14.71, 0.0, 0.0, 3.541};
 constexpr int kTprs[3] = {1, 4, 32};
 constexpr Cost kThreadMapped[3] = {
-    {7.287, 0.06075, 0.008627, 3.755},  // one lane per row (the reference's thread_mapped)
-    {7.055, 0.04398, 0.02554, 2.454},
-    {7.122, 0.006689, 0.1969, 1.709},   // a warp per row
+    {7.099, 0.06098, 0.008628, 3.794},  // one lane per row (the reference's thread_mapped)
+    {6.931, 0.04388, 0.0257, 2.481},
+    {6.782, 0.00683, 0.1977, 1.707},    // a warp per row
 };
 // one lane per row, rows staged through shared memory (thread_mapped
 // variant 1): a candidate where every 32-row chunk fits its buffer (rows of
@@ -97,7 +97,7 @@ constexpr Cost kThreadMapped[3] = {
 // kStagedCoherence of the sampled column pairs step by 0..2), so that the
 // row-aligned x gathers hit L1; on scattered columns the unstaged walk, with
 // more warps resident, hides the gathers' latency better
-constexpr Cost kStaged = {0.0, 0.3045, 0.04461, 0.0};
+constexpr Cost kStaged = {0.0, 0.305, 0.03758, 0.0};
 constexpr int64_t kStagedRows = 27;
 constexpr double kStagedCoherence = 0.5;
 
