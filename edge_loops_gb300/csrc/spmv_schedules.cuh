@@ -212,6 +212,10 @@ __global__ void __launch_bounds__(32 * TmStage<VT>::kWarps)
   unsigned char* const wbase = tm_smem + (size_t)w * 2 * S::kBuf;
   uint64_t pol = 0;  // the matrix streams: evict first, x keeps its L2 lines
   uint32_t ph = 0;   // bit b: the parity of buffer b's next phase
+  // A copy that has not landed within the wait limit: the warp stages
+  // nothing more, sums the rest from global memory, and before it exits
+  // waits (bounded again) for the buffers whose copies were still in flight.
+  uint32_t pending = 0, pending_par = 0;  // bit b: buffer b, its parity
   if (lane == 0) {
     mbar_init(&s_bar[w][0], 1);
     mbar_init(&s_bar[w][1], 1);
@@ -239,7 +243,7 @@ __global__ void __launch_bounds__(32 * TmStage<VT>::kWarps)
   // be summed from global memory (-1; also past the last chunk).
   auto stage = [&](long long qq, const TmRows& r, int buf) {
     int ai = -1;
-    if (qq < nchunks) {
+    if (qq < nchunks && !pending) {
       const long long r0 = qq << 5;
       const int last = (int)((a.rows - r0 < 32 ? a.rows - r0 : 32) - 1);
       const bool mine = lane <= last;
@@ -256,16 +260,13 @@ __global__ void __launch_bounds__(32 * TmStage<VT>::kWarps)
       if (__all_sync(kFullMask, ok) && fits) {
         ai = i0;
         unsigned char* const dst = wbase + (size_t)buf * S::kBuf;
-        // whole 16-byte units; the array's last partial unit, when the chunk
-        // reaches it, is zero-filled past the end
+        // whole 16-byte units by bulk copies, the arrays' last partial
+        // units (in the chunk that reaches their end) by plain loads
         const int* const gi = a.indices + i0;
         const int fi = (int)(ni < ((a.nnz - i0) >> 2) ? ni : ((a.nnz - i0) >> 2));
         const VT* const gv = gvals + v0;
         const long long vleft = (a.nnz - v0) / S::kValPerUnit;
         const int fv = (int)(nv < vleft ? nv : vleft);
-        // two bulk copies by lane 0, completing on the buffer's barrier; the
-        // arrays' last partial units (the chunk that reaches their end) by
-        // plain loads
         if (lane == 0) {
           uint64_t* const bar = &s_bar[w][buf];
           mbar_arrive_expect_tx(bar, 16u * (uint32_t)(fi + fv));
@@ -289,8 +290,11 @@ __global__ void __launch_bounds__(32 * TmStage<VT>::kWarps)
     const int nst = stage(q + nw, nxt, buf ^ 1);
     const TmRows nn = load_rows(q + 2 * nw);
     if (cst >= 0) {
-      if (!mbar_wait_bounded(&s_bar[w][buf], (ph >> buf) & 1u, 2000000000ull)) {
+      const uint32_t par = (ph >> buf) & 1u;
+      if (!__all_sync(kFullMask, mbar_wait_bounded(&s_bar[w][buf], par, 2000000000ull))) {
         if (lane == 0) raise_flag(a.hdr, EL_FLAG_TIMEOUT, (unsigned)q);
+        pending |= 1u << buf;
+        pending_par |= par << buf;
         cst = -1;  // summed from global memory instead
       }
       ph ^= 1u << buf;
@@ -363,6 +367,9 @@ __global__ void __launch_bounds__(32 * TmStage<VT>::kWarps)
     cst = nst;
     buf ^= 1;
   }
+  for (int b = 0; b < 2; ++b)
+    if ((pending >> b) & 1u)
+      mbar_wait_bounded(&s_bar[w][b], (pending_par >> b) & 1u, 2000000000ull);
 }
 
 // ------------------------------------------------------------- group_mapped
