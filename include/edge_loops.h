@@ -359,9 +359,10 @@ el_status el_spmv_edge(el_workspace* ws, const el_coo* A,
  * (plots/data/heuristics.csv), here a cost model of this library's kernels
  * on GB300: estimated times of merge_path and of thread_mapped with 1, 4
  * and 32 lanes per row from (rows, nnz, longest row), and with the row
- * coherence also of one lane per row staged through shared memory.  EL_SCHED_AUTO in
- * el_spmv cannot see the longest row without a synchronisation, so it
- * applies the model with the longest row taken as nnz (the worst case):
+ * coherence also of one lane per row staged through shared memory.
+ * EL_SCHED_AUTO in el_spmv cannot see the longest row without a
+ * synchronisation, so it applies the model with the longest row taken as
+ * nnz (the worst case):
  * merge_path, the choice that is never far off, except for matrices of a
  * few hundred nonzeros; callers that multiply by the same matrix
  * repeatedly call el_spmv_select once and reuse its choice (no cost per
@@ -377,7 +378,8 @@ typedef struct el_row_stats {
                        matrices, near 0 on scattered columns */
 } el_row_stats;
 
-/* Row statistics of A's offsets (one kernel; synchronises `stream`). */
+/* Row statistics of A's offsets, and the coherence from the indices of
+ * sampled rows (one kernel; synchronises `stream`). */
 el_status el_csr_row_stats(el_workspace* ws, const el_csr* A, el_row_stats* out,
                            el_stream_t stream);
 /* The cost model without the coherence (the staged kernel is not weighed):
