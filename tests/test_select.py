@@ -93,6 +93,35 @@ def test_model_quality_on_the_sweep(built_lib):
     assert gm <= float(np.exp(np.log(np.array(loss_plain)).mean()))
 
 
+def test_staged_kernel_rules(built_lib):
+    """el_select_schedule_stats weighs thread_mapped's staged kernel only on
+    rows of at most 27 nonzeros with a row coherence of at least 0.5, and
+    el_select_schedule (no coherence) never picks it."""
+    from edge_loops_gb300 import _lib as L
+    stencil = (1 << 21, 55_742_968)  # the 128^3 stencil's rows and nonzeros
+    assert choose_stats(L, *stencil, 27, 0.84)[0] == "tms"
+    assert choose_stats(L, *stencil, 27, 0.49)[0] != "tms"
+    assert choose_stats(L, *stencil, 28, 0.99)[0] != "tms"
+    assert choose(L, *stencil, 27)[0] != "tms"
+    # merge_path chosen: opts left alone; thread_mapped chosen: its lanes per
+    # row and variant written, the other fields left alone
+    from edge_loops_gb300 import api
+    st = L.ElRowStats()
+    st.max_row_nnz, st.coherence = 100_000, 0.0  # the power-law matrix
+    s, o = C.c_int32(), api.make_opts(items_per_thread=5, variant=1)
+    assert L.lib().el_select_schedule_stats(1 << 20, 1 << 20, 16_000_000, C.byref(st), C.byref(s),
+                                            C.byref(o), None) == L.EL_OK
+    assert (s.value, o.items_per_thread, o.variant) == (L.EL_SCHED_MERGE_PATH_FLAT, 5, 1)
+    st.max_row_nnz, st.coherence = 10, 0.0  # 1000 x 1000, 10 scattered nonzeros per row
+    o = api.make_opts(items_per_thread=5, variant=1)
+    assert L.lib().el_select_schedule_stats(1000, 1000, 10_000, C.byref(st), C.byref(s),
+                                            C.byref(o), None) == L.EL_OK
+    assert s.value == L.EL_SCHED_THREAD_MAPPED
+    assert (o.variant, o.items_per_thread) == (0, 5) and o.threads_per_row in (1, 4, 32)
+    assert L.lib().el_select_schedule_stats(10, 10, 5, None, C.byref(s), C.byref(o),
+                                            None) == L.EL_ERR_NULL_POINTER
+
+
 def test_selection_rules_and_errors(built_lib):
     from edge_loops_gb300 import _lib as L
     assert choose(L, 1 << 20, 16_000_000, 100_000)[0] == "merge_path"  # power-law
