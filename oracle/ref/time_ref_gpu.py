@@ -98,6 +98,12 @@ def main():
         reps = 3 if sched == "thread_mapped" else args.reps
         ms = timed(lambda: api.spmv(A, x, y, schedule=sched, workspace=ws), reps)
         report("edge_loops_gb300", sched, ms)
+    # the schedule el_spmv_select picks (the staged thread_mapped kernel on
+    # short coherent rows such as the stencil's)
+    sel, opts = api.select_schedule(A, workspace=ws)
+    ms = timed(lambda: api.spmv(A, x, y, schedule=sel, workspace=ws, **opts), args.reps)
+    report("edge_loops_gb300", sel + "".join(f" {k}={v}" for k, v in opts.items()), ms,
+           "the schedule el_spmv_select picks")
 
 
 def spmm(args):
